@@ -1,0 +1,215 @@
+"""Pin the CPU oracle against the reference's own outputs (no GPU needed).
+
+The golden vectors were produced by the reference itself (its headers compiled
+by oracle/build_ref.sh, one OpenMP thread) and its field generator; see
+tests/golden/make_golden.py. The oracle is the checker of every GPU parity
+test, so it must reproduce them exactly.
+"""
+
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import two_phase
+
+
+def _sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("key", ["n64_s0_12_3", "n1024_s1_1000_0.001", "n128_s0_12_3", "n32_s5_12_3",
+                                 "n128_s3_100_0.01", "n512_s7_100_0.01", "n64_s13_1e+06_1"])
+def test_field_generator_reproduces_reference_bits(golden, key: str) -> None:
+    from darcy_cpp_gb300.fields import gaussian_random_field, two_phase_permeability
+
+    _, meta = golden
+    spec = meta["fields"][key]
+    grf = gaussian_random_field(spec["n"], seed=spec["seed"])
+    assert _sha(grf) == spec["grf_sha256"]
+    assert _sha(two_phase_permeability(grf, spec["hi"], spec["lo"])) == spec["sha256"]
+
+
+def test_field_generator_alpha_tau(golden) -> None:
+    from darcy_cpp_gb300.fields import gaussian_random_field
+
+    _, meta = golden
+    assert _sha(gaussian_random_field(16, alpha=1.5, tau=2.0, seed=3)) == meta["fields"]["grf_alpha1.5_n16_s3"]["sha256"]
+
+
+def _kwargs(spec: dict) -> dict:
+    return dict(spec["kwargs"])
+
+
+def _field_for(name: str, arrays: dict, n: int) -> tuple[np.ndarray, object]:
+    if name == "cfg1":
+        return arrays["a_cfg1"], 1.0
+    if name.startswith("tiny"):
+        return np.full((n, n), 2.0), 1.0
+    if name == "fvar32":
+        return two_phase(32, 3), arrays["f_var32"]
+    if name == "maxiter2_128":
+        return two_phase(128, 0), 1.0
+    if name == "contrast1e6_64":
+        return two_phase(64, 13, 1e6, 1.0), 1.0
+    if name.startswith("n48_c"):
+        return two_phase(48, 4), 1.0
+    if name.startswith("table"):
+        return two_phase(n, 0), 1.0
+    if name == "cfg5_128_s3":
+        return two_phase(128, 3, 1e2, 1e-2), 1.0
+    if name == "cfg2_1024":
+        return two_phase(1024, 1, 1e3, 1e-3), 1.0
+    return two_phase(n, n), 1.0
+
+
+SMALL_CASES = ["cfg1", "tiny1", "tiny2", "tiny3", "tiny4", "tiny5", "fvar32", "maxiter2_128",
+               "contrast1e6_64", "table128"] + [f"n{n}_{pc}" for n in (16, 17, 31, 32, 33, 48)
+                                                for pc in ("multigrid", "jacobi", "none")] + [
+    f"n48_c{c}_s{s}" for c in (1, 2) for s in (1, 2, 3)]
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_oracle_solve_matches_reference(golden, orc, name: str) -> None:
+    arrays, meta = golden
+    spec = meta["solves"][name]
+    a, f = _field_for(name, arrays, spec["n"])
+    out = orc.solve(a, f, **_kwargs(spec))
+    assert out["iterations"] == spec["iterations"]
+    assert out["levels"] == spec["levels"]
+    assert out["converged"] == spec["converged"]
+    assert out["residual"] == spec["residual"]  # one thread: same reduction order, same bits
+    assert out["u"].sum() == spec["u_sum"]
+    if f"u_{name}" in arrays:
+        assert np.array_equal(out["u"], arrays[f"u_{name}"])
+    if spec["kwargs"].get("record_history"):
+        assert np.array_equal(out["history"], np.array(spec["history"]))
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("name", ["table256", "table512", "cfg5_128_s3", "cfg2_1024"])
+def test_oracle_solve_matches_reference_large(golden, orc, name: str) -> None:
+    arrays, meta = golden
+    spec = meta["solves"][name]
+    a, f = _field_for(name, arrays, spec["n"])
+    orc.set_threads(8)
+    try:
+        out = orc.solve(a, f, **_kwargs(spec))
+    finally:
+        orc.set_threads(1)
+    assert out["iterations"] == spec["iterations"]
+    assert out["levels"] == spec["levels"]
+    # Many threads change the reduction order; at 1e6 contrast the last
+    # residual moves by several per cent while u agrees to ~1e-14.
+    assert out["residual"] < spec["kwargs"]["tol"]
+    assert abs(out["residual"] - spec["residual"]) <= 0.25 * spec["residual"]
+    assert abs(out["u"].sum() - spec["u_sum"]) <= 1e-10 * abs(spec["u_sum"])
+
+
+def test_oracle_apply_operator_matches_reference(golden, orc) -> None:
+    arrays, _ = golden
+    assert np.array_equal(orc.apply_operator(arrays["a_op17"], arrays["x_op17"]), arrays["y_op17"])
+
+
+@pytest.mark.parametrize("cycle", [1, 2])
+@pytest.mark.parametrize("sweeps", [1, 2, 3])
+def test_oracle_apply_preconditioner_matches_reference(golden, orc, cycle: int, sweeps: int) -> None:
+    arrays, _ = golden
+    z = orc.apply_preconditioner(arrays["a_pc32"], arrays["r_pc32"], pre_sweeps=sweeps,
+                                 post_sweeps=sweeps, cycle_index=cycle)
+    assert np.array_equal(z, arrays[f"z_pc32_c{cycle}_s{sweeps}"])
+    assert np.array_equal(orc.apply_preconditioner(arrays["a_pc33"], arrays["r_pc33"]), arrays["z_pc33"])
+
+
+def test_oracle_hierarchy_matches_reference(golden, orc) -> None:
+    """Galerkin coarsening by face sums (level.hpp:171-211), every level, bitwise.
+
+    The reference dump recovers faces through apply(), so only interior faces
+    (those that couple two cells) are compared; diag and inv_diag fully.
+    """
+    arrays, _ = golden
+    levels = orc.hierarchy(arrays["a_h13"])
+    assert [L["e"].shape[0] for L in levels] == [13, 7, 4, 2, 1]
+    for lvl, L in enumerate(levels):
+        m = L["e"].shape[0]
+        assert np.array_equal(L["diag"], arrays[f"h13_l{lvl}_diag"])
+        assert np.array_equal(L["inv_diag"], arrays[f"h13_l{lvl}_inv_diag"])
+        assert np.array_equal(L["e"][:, : m - 1], arrays[f"h13_l{lvl}_e"][:, : m - 1])
+        assert np.array_equal(L["w"][:, 1:], arrays[f"h13_l{lvl}_w"][:, 1:])
+        assert np.array_equal(L["n"][: m - 1], arrays[f"h13_l{lvl}_n"][: m - 1])
+        assert np.array_equal(L["s"][1:], arrays[f"h13_l{lvl}_s"][1:])
+
+
+def test_oracle_galerkin_identity(orc) -> None:
+    """coarsen() == P^T A P entry-wise (reference tests/cpp/test_core.cpp:132-163)."""
+    rng = np.random.default_rng(8)
+    for n in (6, 7, 8, 13):
+        a = np.where(rng.random((n, n)) < 0.5, 3.0, 12.0)
+        nc = (n + 1) // 2
+        dense = np.stack([orc.apply_operator(a, np.eye(n * n)[k].reshape(n, n)).ravel()
+                          for k in range(n * n)], axis=1)
+        P = np.zeros((n * n, nc * nc))
+        for k in range(n * n):
+            P[k, (k // n // 2) * nc + (k % n) // 2] = 1.0
+        galerkin = P.T @ dense @ P
+        L = orc.hierarchy(a)[1]
+        coarse = np.diag(L["diag"].ravel())
+        for K in range(nc * nc):
+            I, J = divmod(K, nc)
+            if J + 1 < nc:
+                coarse[K, K + 1] = -L["e"][I, J]
+            if J > 0:
+                coarse[K, K - 1] = -L["w"][I, J]
+            if I + 1 < nc:
+                coarse[K, K + nc] = -L["n"][I, J]
+            if I > 0:
+                coarse[K, K - nc] = -L["s"][I, J]
+        assert np.abs(galerkin - coarse).max() < 1e-12
+
+
+def test_oracle_batch_matches_serial(golden, orc) -> None:
+    arrays, meta = golden
+    batch = orc.solve_batch(arrays["batch_a32"], tol=1e-12, threads=2)
+    assert list(batch["iterations"]) == meta["batch32_iterations"]
+    for i, a in enumerate(arrays["batch_a32"]):
+        assert np.allclose(batch["u"][i], orc.solve(a, tol=1e-12)["u"], atol=1e-13, rtol=0)
+
+
+def test_oracle_validation_messages(orc) -> None:
+    a = np.full((8, 8), 2.0)
+    a[3, 4] = -1.0
+    with pytest.raises(orc.OracleError, match="positive.*flat index 28"):
+        orc.solve(a)
+    with pytest.raises(orc.OracleError, match="tol must be positive"):
+        orc.solve(np.ones((4, 4)), tol=0.0)
+    with pytest.raises(orc.OracleError, match="max_iter"):
+        orc.solve(np.ones((4, 4)), max_iter=0)
+    with pytest.raises(orc.OracleError, match="cycle_index"):
+        orc.solve(np.ones((4, 4)), cycle_index=3)
+
+
+def test_oracle_matches_reference_build_directly(orc) -> None:
+    """When the reference compiled here (oracle/_ref), compare on fresh inputs too."""
+    if not orc.have_ref():
+        pytest.skip("oracle/_ref not built (reference checkout absent)")
+    orc.ref_set_threads(1)
+    rng = np.random.default_rng(99)
+    for n in (9, 24, 37, 64):
+        a = np.exp(rng.normal(0, 2.0, (n, n)))
+        f = rng.standard_normal((n, n))
+        ours = orc.solve(a, f, tol=1e-11, cycle_index=1 + n % 2)
+        ref = orc.ref_solve(a, f, tol=1e-11, cycle_index=1 + n % 2)
+        assert ours["iterations"] == ref["iterations"]
+        assert np.array_equal(ours["u"], ref["u"])
+
+
+def test_oracle_warm_start_from_solution_converges_immediately(orc) -> None:
+    a = two_phase(32, 1)
+    u = orc.solve(a, tol=1e-12)["u"]
+    warm = orc.solve(a, tol=1e-10, u0=u)
+    assert warm["converged"] and warm["iterations"] == 0
+    cold = orc.solve(a, tol=1e-10)
+    half = orc.solve(a, tol=1e-10, u0=0.5 * u)
+    assert half["converged"] and half["iterations"] <= cold["iterations"]
