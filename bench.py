@@ -1,0 +1,353 @@
+"""Benchmark of the darcy MG-PCG solve path on GB300 (one JSON line on stdout).
+
+Headline workload (the reference's single large solve): 1024 x 1024 cells,
+permeability = two-phase threshold of the Gaussian random field with seed 1,
+a in {1e3, 1e-3} (1e6 contrast), f = 1, W-cycle MG-PCG to relative residual
+1e-10. A step is one such solve; `value` is ms/solve with the inputs already
+resident in HBM, `e2e` the same through the package API from host arrays.
+The chosen form (FP32 cycle inside FP64 CG) is compared with the plain FP64
+form, and the 64 x 64 batched solves/s (the other half of the metric) are
+reported beside it, both forms, through the batched engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU oracle (the reference algorithm restated in
+C with the reference's OpenMP structure) on all host cores for the same
+workload. Data: synthetic fields from the reference's generator construction.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "64² solves/s & 1024² ms/solve at rel-res 1e-10: chosen form vs plain FP64"
+N_BIG, SEED_BIG, HI_BIG, LO_BIG = 1024, 1, 1e3, 1e-3
+N_SMALL, BATCH_SMALL = 64, 4096
+TOL = 1e-10
+L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+
+
+def field(n: int, seed: int, hi: float, lo: float) -> np.ndarray:
+    from darcy_cpp_gb300.fields import gaussian_random_field, two_phase_permeability
+
+    return two_phase_permeability(gaussian_random_field(n, seed=seed), hi=hi, lo=lo)
+
+
+def small_batch(count: int) -> np.ndarray:
+    return np.stack([field(N_SMALL, s, 12.0, 3.0) for s in range(count)])
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int) -> None:
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc) -> None:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- GPU (ours)
+
+def load_peaks() -> dict:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return {"hbm_gbs": float(data["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def run_ours(args, rank: int, world: int) -> dict | None:
+    import torch
+
+    import darcy_cpp_gb300 as darcy
+    from darcy_cpp_gb300 import capi
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    ctx = capi.Context(dev)
+    stream = torch.cuda.current_stream()
+
+    a_big = field(N_BIG, SEED_BIG, HI_BIG, LO_BIG)
+    m = a_big.size
+    d_a = torch.from_numpy(a_big).to(f"cuda:{dev}")
+    d_u = torch.empty_like(d_a)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def device_solve(form: str) -> tuple[float, object]:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        e0.record(stream)
+        st = ctx.solve_device(d_a.data_ptr(), N_BIG, d_u.data_ptr(), stream.cuda_stream, tol=TOL, form=form)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), st
+
+    def e2e_solve(form: str) -> tuple[float, object]:
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = darcy.solve(a_big, tol=TOL, form=form)
+        return (time.perf_counter() - t0) * 1e3, res
+
+    out: dict = {}
+    # warm-up: graph capture, plan allocation, clocks
+    for _ in range(max(args.warmup, 3)):
+        for form in ("mixed", "fp64"):
+            device_solve(form)
+            e2e_solve(form)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    with ClockSampler(dev) as clocks:
+        times = {"mixed": [], "fp64": []}
+        stats = {}
+        for _ in range(args.steps):
+            for form in ("mixed", "fp64"):
+                ms, st = device_solve(form)
+                times[form].append(ms)
+                stats[form] = st
+        e2e = {"mixed": [], "fp64": []}
+        e2e_res = {}
+        for _ in range(args.steps):
+            for form in ("mixed", "fp64"):
+                ms, res = e2e_solve(form)
+                e2e[form].append(ms)
+                e2e_res[form] = res
+        # 64 x 64 batch (the solves/s half of the metric)
+        batch = small_batch(BATCH_SMALL)
+        darcy.solve_batch(batch[:256], tol=TOL, form="mixed")
+        darcy.solve_batch(batch[:256], tol=TOL, form="fp64")
+        bt = {}
+        for form in ("mixed", "fp64"):
+            runs = []
+            for _ in range(max(1, args.steps // 2)):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                br = darcy.solve_batch(batch, tol=TOL, form=form)
+                runs.append(time.perf_counter() - t0)
+            bt[form] = (min(runs), br)
+    total_ms = {k: sum(v) for k, v in times.items()}
+    if world > 1:
+        t = torch.tensor([total_ms["mixed"], total_ms["fp64"]], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = {"mixed": float(t[0]), "fp64": float(t[1])}
+    if rank != 0:
+        return None
+
+    ms_mixed = total_ms["mixed"] / (args.steps * world)
+    ms_fp64 = total_ms["fp64"] / (args.steps * world)
+    e2e_mixed = statistics.median(e2e["mixed"])
+    st_m, st_p = stats["mixed"], stats["fp64"]
+    ref_u = e2e_res["fp64"].u
+    mixed_err = float(np.linalg.norm(e2e_res["mixed"].u - ref_u) / np.linalg.norm(ref_u))
+
+    prof = ctx.profile_kernels(a_big, reps=20, tol=TOL, form="mixed")
+    for row in prof:
+        row["share_ms"] = row["avg_ms"] * row["launches_per_iteration"]
+    peaks = load_peaks()
+    dom = max(prof, key=lambda k: k["share_ms"])
+    achieved = dom["bytes"] / (dom["avg_ms"] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "peak_source": peaks["source"], "avg_launch_us": round(dom["avg_ms"] * 1e3, 3),
+                "algorithmic_bytes_per_launch": dom["bytes"],
+                "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()} for p in prof]}
+
+    cpu = run_cpu_baseline(sample_solves=1)
+    bsm = BATCH_SMALL / bt["mixed"][0]
+    bsp = BATCH_SMALL / bt["fp64"][0]
+    line = {
+        "metric": METRIC,
+        "value": round(ms_mixed, 3),
+        "unit": "ms/solve",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_mixed, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 CG + f32 cycle",
+        "data": "synthetic: two-phase GRF fields (reference generator construction), seeded",
+        "config": {"workload": "1024x1024 single solve, GRF seed 1, a in {1e3,1e-3}, f=1, W-cycle, tol 1e-10",
+                   "form": "mixed (FP32 V/W-cycle inside FP64 CG)", "l2": "flushed between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "iterations": {"mixed": st_m.iterations, "fp64": st_p.iterations},
+        "true_residual": {"mixed": st_m.true_residual, "fp64": st_p.true_residual},
+        "mixed_vs_fp64_rel_l2": mixed_err,
+        "plain_fp64": {"value": round(ms_fp64, 3), "unit": "ms/solve",
+                       "e2e": round(statistics.median(e2e["fp64"]), 3)},
+        "chosen_vs_plain": round(ms_fp64 / ms_mixed, 3),
+        "batch64": {"metric": "64x64 solves/s (4096 problems, seeds 0..4095, {12,3})",
+                    "mixed": round(bsm, 1), "fp64": round(bsp, 1), "unit": "solves/s",
+                    "chosen_vs_plain": round(bsm / bsp, 3),
+                    "mean_iterations": float(bt["mixed"][1].iterations.mean()),
+                    "e2e": True, "h2d_bytes": int(batch.nbytes), "d2h_bytes": int(batch.nbytes)},
+        "e2e": {"value": round(e2e_mixed, 3), "unit": "ms/solve", "h2d_bytes_per_step": int(8 * m),
+                "d2h_bytes_per_step": int(8 * m + 64)},
+        "gpu_launches": int(st_m.kernel_launches),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+    return line
+
+
+# ------------------------------------------------------- CPU (the oracle)
+
+def run_cpu_baseline(sample_solves: int = 1) -> dict:
+    """The reference algorithm (oracle C port, OpenMP) on all host cores."""
+    import oracle
+
+    cores = oracle.cpu_count()
+    oracle.set_threads(cores)
+    a = field(N_BIG, SEED_BIG, HI_BIG, LO_BIG)
+    best = float("inf")
+    it = 0
+    for _ in range(sample_solves):
+        t0 = time.perf_counter()
+        out = oracle.solve(a, tol=TOL)
+        best = min(best, time.perf_counter() - t0)
+        it = out["iterations"]
+    batch = small_batch(256)
+    t0 = time.perf_counter()
+    oracle.solve_batch(batch, tol=TOL, threads=cores)
+    bsec = time.perf_counter() - t0
+    return {"value": round(best * 1e3, 2), "unit": "ms/solve", "cores": cores, "kind": "port",
+            "sample": f"{sample_solves} solve(s) of the 1024x1024 workload ({it} iterations), min; "
+                      f"64x64 batch of 256: {256 / bsec:.1f} solves/s",
+            "batch64_solves_per_s": round(256 / bsec, 1)}
+
+
+def run_reference(args, rank: int, world: int) -> dict | None:
+    if rank != 0:
+        return None
+    import oracle
+
+    cores = oracle.cpu_count()
+    oracle.set_threads(cores)
+    a = field(N_BIG, SEED_BIG, HI_BIG, LO_BIG)
+    for _ in range(min(args.warmup, 1)):
+        oracle.solve(a, tol=TOL)
+    steps = max(1, min(args.steps, 5))
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        out = oracle.solve(a, tol=TOL)
+        times.append((time.perf_counter() - t0) * 1e3)
+    batch = small_batch(1024)
+    oracle.solve_batch(batch[:64], tol=TOL, threads=cores)
+    t0 = time.perf_counter()
+    oracle.solve_batch(batch, tol=TOL, threads=cores)
+    bsec = time.perf_counter() - t0
+    value = sum(times) / len(times)
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "ms/solve",
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(value, 2),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: two-phase GRF fields (reference generator construction), seeded",
+        "config": {"workload": "1024x1024 single solve, GRF seed 1, a in {1e3,1e-3}, f=1, W-cycle, tol 1e-10",
+                   "form": "reference algorithm on the host CPU (oracle C port, OpenMP)"},
+        "iterations": out["iterations"],
+        "batch64": {"metric": "64x64 solves/s (1024 problems, seeds 0..1023, {12,3})",
+                    "value": round(1024 / bsec, 1), "unit": "solves/s"},
+        "cpu_baseline": {"value": round(value, 2), "unit": "ms/solve", "cores": cores, "kind": "port",
+                         "sample": f"{steps} solve(s) of the 1024x1024 workload, mean"},
+        "e2e": {"value": round(value, 2), "unit": "ms/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    line = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

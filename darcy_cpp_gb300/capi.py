@@ -1,0 +1,194 @@
+"""ctypes binding of the C ABI (include/darcy_gpu.h).
+
+This is the binding a caller without the pybind11 extension would write -- the
+same shape as the `ctypes` stub in INTEGRATION.md -- and the route the
+benchmark and the C-ABI tests use: plain pointers and sizes, host or device
+buffers, status codes, `dgpu_last_error()` for messages.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libdarcy_gpu.so"
+
+OK, INVALID_INPUT, CUDA_ERROR, NO_MEMORY, TIMEOUT = 0, 1, 2, 3, 4
+PC = {"none": 0, "jacobi": 1, "multigrid": 2, "mg": 2}
+FORM = {"fp64": 0, "plain": 0, "mixed": 1}
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("preconditioner", ctypes.c_int),
+                ("pre_sweeps", ctypes.c_int), ("post_sweeps", ctypes.c_int), ("cycle_index", ctypes.c_int),
+                ("record_history", ctypes.c_int), ("form", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("residual", ctypes.c_double), ("converged", ctypes.c_int),
+                ("levels", ctypes.c_int), ("history_len", ctypes.c_int), ("true_residual", ctypes.c_double),
+                ("device_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64)]
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("avg_ms", ctypes.c_double), ("bytes", ctypes.c_double),
+                ("launches_per_iteration", ctypes.c_double)]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_lib = None
+
+
+class DarcyGpuError(RuntimeError):
+    pass
+
+
+class InvalidInput(ValueError):
+    pass
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(str(LIB_PATH))
+        L.dgpu_last_error.restype = ctypes.c_char_p
+        L.dgpu_create.argtypes = [ctypes.c_int, ctypes.POINTER(_P)]
+        L.dgpu_destroy.argtypes = [_P]
+        L.dgpu_destroy.restype = None
+        L.dgpu_device_info.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
+        L.dgpu_solve.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int64, ctypes.POINTER(Options), _P, _P, _P,
+                                 ctypes.POINTER(Stats)]
+        L.dgpu_solve_device.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int64, ctypes.POINTER(Options), _P,
+                                        _P, ctypes.POINTER(Stats), _P]
+        L.dgpu_solve_batch.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
+                                       ctypes.POINTER(Options), _P, _P, _P, _P, _P, _P]
+        L.dgpu_solve_uneven.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.c_double, ctypes.POINTER(Options),
+                                        _P, _P, _P, _P, _P, _P]
+        L.dgpu_apply_operator.argtypes = [_P, _P, _P, ctypes.c_int64, _P]
+        L.dgpu_apply_preconditioner.argtypes = [_P, _P, _P, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_int, _P]
+        L.dgpu_hierarchy.argtypes = [_P, _P, ctypes.c_int64, _P, ctypes.c_int64]
+        L.dgpu_hierarchy.restype = ctypes.c_int64
+        L.dgpu_num_levels.argtypes = [ctypes.c_int64]
+        L.dgpu_profile_kernels.argtypes = [_P, _P, ctypes.c_int64, ctypes.POINTER(Options), ctypes.c_int,
+                                           ctypes.POINTER(KernelTime), ctypes.c_int, _I]
+        L.dgpu_flush_l2.argtypes = [_P, ctypes.c_int64]
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc == OK:
+        return
+    msg = lib().dgpu_last_error().decode()
+    if rc == INVALID_INPUT:
+        raise InvalidInput(msg)
+    raise DarcyGpuError(f"status {rc}: {msg}")
+
+
+def options(tol=1e-10, max_iter=10000, preconditioner="multigrid", pre_sweeps=1, post_sweeps=1, cycle_index=2,
+            record_history=False, form="fp64") -> Options:
+    return Options(float(tol), int(max_iter), PC[preconditioner], int(pre_sweeps), int(post_sweeps),
+                   int(cycle_index), int(bool(record_history)), FORM[form])
+
+
+def _ptr(arr: np.ndarray | None):
+    return None if arr is None else ctypes.c_void_p(arr.ctypes.data)
+
+
+def _f64(x) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+
+
+class Context:
+    """Owns one dgpu_context (stream, device buffers, captured graphs)."""
+
+    def __init__(self, device: int = -1) -> None:
+        self.handle = _P()
+        check(lib().dgpu_create(int(device), ctypes.byref(self.handle)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().dgpu_destroy(self.handle)
+            self.handle = _P()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        check(lib().dgpu_device_info(self.handle, buf, 512))
+        return buf.value.decode()
+
+    def solve(self, a, f=1.0, x0=None, **kw) -> dict:
+        a = _f64(a)
+        n = a.shape[0]
+        fa = None if np.isscalar(f) else _f64(f)
+        u = np.empty_like(a)
+        opt = options(**kw)
+        hist = np.empty(opt.max_iter + 1) if opt.record_history else None
+        st = Stats()
+        check(lib().dgpu_solve(self.handle, _ptr(a), _ptr(fa), float(f) if fa is None else 0.0, n,
+                               ctypes.byref(opt), _ptr(None if x0 is None else _f64(x0)), _ptr(u), _ptr(hist),
+                               ctypes.byref(st)))
+        return {"u": u, "iterations": st.iterations, "residual": st.residual, "converged": bool(st.converged),
+                "levels": st.levels, "true_residual": st.true_residual, "device_ms": st.device_ms,
+                "kernel_launches": st.kernel_launches,
+                "history": hist[: st.history_len].copy() if hist is not None else np.empty(0)}
+
+    def solve_device(self, d_a: int, n: int, d_u: int, stream: int | None = None, f_scalar: float = 1.0,
+                     **kw) -> Stats:
+        """Solve on device-resident buffers (raw device pointers)."""
+        opt = options(**kw)
+        st = Stats()
+        check(lib().dgpu_solve_device(self.handle, ctypes.c_void_p(d_a), None, float(f_scalar), int(n),
+                                      ctypes.byref(opt), None, ctypes.c_void_p(d_u), ctypes.byref(st),
+                                      ctypes.c_void_p(stream) if stream else None))
+        return st
+
+    def solve_batch(self, a, f=1.0, **kw) -> dict:
+        a = _f64(a)
+        batch, n = a.shape[0], a.shape[1]
+        fa = None if np.isscalar(f) else _f64(f)
+        u = np.empty_like(a)
+        it = np.zeros(batch, dtype=np.int32)
+        res = np.zeros(batch)
+        conv = np.zeros(batch, dtype=np.int32)
+        lev = np.zeros(batch, dtype=np.int32)
+        opt = options(**kw)
+        check(lib().dgpu_solve_batch(self.handle, _ptr(a), _ptr(fa), float(f) if fa is None else 0.0, 0, batch, n,
+                                     ctypes.byref(opt), None, _ptr(u), _ptr(it), _ptr(res), _ptr(conv), _ptr(lev)))
+        return {"u": u, "iterations": it, "residuals": res, "converged": conv.astype(bool), "levels": lev}
+
+    def apply_operator(self, a, x) -> np.ndarray:
+        a, x = _f64(a), _f64(x)
+        y = np.empty_like(x)
+        check(lib().dgpu_apply_operator(self.handle, _ptr(a), _ptr(x), a.shape[0], _ptr(y)))
+        return y
+
+    def apply_preconditioner(self, a, r, pre_sweeps=1, post_sweeps=1, cycle_index=2, form="fp64") -> np.ndarray:
+        a, r = _f64(a), _f64(r)
+        z = np.empty_like(r)
+        check(lib().dgpu_apply_preconditioner(self.handle, _ptr(a), _ptr(r), a.shape[0], pre_sweeps, post_sweeps,
+                                              cycle_index, FORM[form], _ptr(z)))
+        return z
+
+    def profile_kernels(self, a, reps: int = 20, **kw) -> list[dict]:
+        a = _f64(a)
+        rows = (KernelTime * 32)()
+        count = ctypes.c_int()
+        opt = options(**kw)
+        check(lib().dgpu_profile_kernels(self.handle, _ptr(a), a.shape[0], ctypes.byref(opt), int(reps), rows, 32,
+                                         ctypes.byref(count)))
+        return [{"name": r.name.decode(), "avg_ms": r.avg_ms, "bytes": r.bytes,
+                 "launches_per_iteration": r.launches_per_iteration} for r in rows[: count.value]]
+
+    def flush_l2(self, nbytes: int = 512 << 20) -> None:
+        check(lib().dgpu_flush_l2(self.handle, int(nbytes)))

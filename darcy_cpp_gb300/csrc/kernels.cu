@@ -1,0 +1,851 @@
+// sm_103a kernels of the darcy GB300 engine.
+//
+// Two engines share the level operations of common.cuh:
+//   * the grid engine (one solve spread over the whole GPU): one kernel per
+//     phase on the large levels, the coarse tail handed to one CTA, the PCG
+//     scalars kept on the device so that no iteration waits for the host;
+//   * the block engine (batched solves): one CTA runs a whole PCG solve of one
+//     problem, pulling problems from a work counter, largest first.
+#include <math.h>
+
+#include "cycle.cuh"
+#include "engine.h"
+
+namespace dgpu {
+
+// ------------------------------------------------------------ small helpers
+
+static inline int grid_for(int64_t work, int threads = kThreads) {
+    int64_t g = (work + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > kMaxBlocks) g = kMaxBlocks;
+    return (int)g;
+}
+
+__device__ __forceinline__ void stop_loop(CgState* st) {
+    if (st->use_cond) cudaGraphSetConditional(st->cond, 0u);
+}
+
+// Two-value variant of grid_sum_last.
+__device__ __forceinline__ bool grid_sum2_last(double v1, double v2, double* partials, unsigned* ticket,
+                                               double* scratch, double& t1, double& t2) {
+    __shared__ bool s_last;
+    const double b1 = block_sum(v1, scratch);
+    const double b2 = block_sum(v2, scratch);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = b1;
+        partials[2 * blockIdx.x + 1] = b2;
+        __threadfence();
+        s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double a1 = 0.0, a2 = 0.0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+        a1 += ((volatile double*)partials)[2 * q];
+        a2 += ((volatile double*)partials)[2 * q + 1];
+    }
+    t1 = block_sum(a1, scratch);
+    t2 = block_sum(a2, scratch);
+    if (threadIdx.x == 0) *ticket = 0;
+    return true;
+}
+
+// y = A x at one cell, FP64 (level.hpp:105-119).
+__device__ __forceinline__ double apply_cell(const Lvl64& L, const double* __restrict__ x, int i, int j) {
+    const int n = L.n;
+    const int64_t k = (int64_t)i * n + j;
+    double v = L.d[k] * x[k];
+    if (j + 1 < n) v -= L.e[k] * x[k + 1];
+    if (j > 0) v -= L.e[k - 1] * x[k - 1];
+    if (i + 1 < n) v -= L.nf[k] * x[k + n];
+    if (i > 0) v -= L.nf[k - n] * x[k - n];
+    return v;
+}
+
+// ------------------------------------------------------------- setup kernels
+
+__global__ void k_build_fine(const double* __restrict__ a, Lvl64 L, unsigned long long* bad) {
+    build_fine<GridScope>(a, L, bad);
+}
+__global__ void k_coarsen(Lvl64 F, Lvl64 C) { coarsen<GridScope>(F, C); }
+__global__ void k_to_fp32(Lvl64 L, float* e, float* nf, float* d, float* id) {
+    to_fp32<GridScope>(L, e, nf, d, id);
+}
+
+void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad, cudaStream_t s) {
+    k_build_fine<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(a, L, bad);
+}
+void launch_coarsen(const Lvl64& F, const Lvl64& C, cudaStream_t s) {
+    k_coarsen<<<grid_for((int64_t)C.n * C.n), kThreads, 0, s>>>(F, C);
+}
+void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, cudaStream_t s) {
+    k_to_fp32<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, e, nf, d, id);
+}
+
+// ---------------------------------------------------------------- PCG kernels
+
+// b = f h^2 (solver.hpp:98-102), r = b (or b - A u0 for a warm start), u = 0
+// (or u0), p = 0, ||b|| and the initial residual (solver.hpp:104-108, :143-144).
+__global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
+                          double* __restrict__ b, double* __restrict__ r, double* __restrict__ u,
+                          double* __restrict__ p, float* __restrict__ b0f, const double* __restrict__ u0,
+                          Lvl64 L0, CgState* st, double* partials) {
+    __shared__ double red[32];
+    double sb = 0.0, sr = 0.0;
+    const int n = L0.n;
+    const double fscalar = st->fscalar;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        const double bk = (f ? f[k] : fscalar) * h2;
+        double rk = bk;
+        if (u0) {
+            const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+            rk = bk - apply_cell(L0, u0, i, j);
+            u[k] = u0[k];
+        } else {
+            u[k] = 0.0;
+        }
+        b[k] = bk;
+        r[k] = rk;
+        p[k] = 0.0;
+        if (b0f) b0f[k] = (float)rk;
+        sb += bk * bk;
+        sr += rk * rk;
+    }
+    double tb, tr;
+    if (!grid_sum2_last(sb, sr, partials, &st->ticket[0], red, tb, tr)) return;
+    if (threadIdx.x == 0) {
+        st->bnorm = sqrt(tb);
+        st->it = 0;
+        st->beta = 0.0;
+        st->converged = 0;
+        st->done = 0;
+        if (st->bad != ~0ull) {  // invalid permeability: reported by the host, no iteration
+            st->residual = 0.0;
+            st->done = 1;
+        } else if (st->bnorm == 0.0) {  // f == 0: u == 0 exactly, no iteration
+            st->residual = 0.0;
+            st->converged = 1;
+            st->done = 1;
+        } else {
+            st->residual = u0 ? sqrt(tr) / st->bnorm : 1.0;
+            if (u0 && st->residual < st->tol) {
+                st->converged = 1;
+                st->done = 1;
+            }
+        }
+        if (st->record_history && st->history) st->history[0] = st->residual;
+    }
+}
+
+// Level kernels: each returns at once when the solve has finished, so a
+// converged iteration's remaining graph nodes cost only their launch.
+template <class T>
+__global__ void k_gs(Lvl<T> L, int c, bool zero, const CgState* st) {
+    if (st && st->done) return;
+    gs_colour<GridScope>(L, c, zero);
+}
+template <class T>
+__global__ void k_residual_restrict(Lvl<T> L, T* bc, const CgState* st) {
+    if (st && st->done) return;
+    residual_restrict<GridScope>(L, bc);
+}
+template <class T>
+__global__ void k_prolong_gs1(Lvl<T> L, const T* xc, const CgState* st) {
+    if (st && st->done) return;
+    prolong_gs1<GridScope>(L, xc);
+}
+
+// Last post-smoothing pass on level 0 (colour 0) fused with rz = r . z and
+// beta = rz_new / rz (solver.hpp:167-171). z is the level-0 iterate; in the
+// mixed form it is the FP32 iterate widened to FP64 on the fly.
+template <class T>
+__global__ void k_gs0_dot(Lvl<T> L, const double* __restrict__ r, CgState* st, double* partials) {
+    __shared__ double red[32];
+    if (st->done) return;
+    const int n = L.n;
+    double acc = 0.0;
+    const int64_t cnt0 = colour_count(n, 0);
+    for (int64_t t = GridScope::start(); t < cnt0; t += GridScope::stride()) {
+        int i, j;
+        colour_cell(n, 0, t, i, j);
+        const int64_t k = (int64_t)i * n + j;
+        T v = L.b[k];
+        if (j + 1 < n) v += L.e[k] * L.x[k + 1];
+        if (j > 0) v += L.e[k - 1] * L.x[k - 1];
+        if (i + 1 < n) v += L.nf[k] * L.x[k + n];
+        if (i > 0) v += L.nf[k - n] * L.x[k - n];
+        const T xn = v * L.id[k];
+        L.x[k] = xn;
+        acc += r[k] * (double)xn;
+    }
+    const int64_t cnt1 = colour_count(n, 1);
+    for (int64_t t = GridScope::start(); t < cnt1; t += GridScope::stride()) {
+        int i, j;
+        colour_cell(n, 1, t, i, j);
+        const int64_t k = (int64_t)i * n + j;
+        acc += r[k] * (double)L.x[k];
+    }
+    double tot;
+    if (!grid_sum_last(acc, partials, &st->ticket[1], red, tot)) return;
+    if (threadIdx.x == 0) {
+        st->beta = st->it == 0 ? 0.0 : (tot - st->rzo) / st->rz;
+        st->rz = tot;
+    }
+}
+
+// rz = r . z after a preconditioner that ended elsewhere (coarse-tail-only
+// hierarchies).
+template <class T>
+__global__ void k_dot_rz(const T* __restrict__ z, const double* __restrict__ r, int64_t m, CgState* st,
+                         double* partials) {
+    __shared__ double red[32];
+    if (st->done) return;
+    double acc = 0.0;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) acc += r[k] * (double)z[k];
+    double tot;
+    if (!grid_sum_last(acc, partials, &st->ticket[1], red, tot)) return;
+    if (threadIdx.x == 0) {
+        st->beta = st->it == 0 ? 0.0 : (tot - st->rzo) / st->rz;
+        st->rz = tot;
+    }
+}
+
+// Jacobi (z = r / d) or no preconditioner (z = r), with rz and beta
+// (solver.hpp:122-137, :167-171). id == null selects "none".
+__global__ void k_precond_diag(const double* __restrict__ r, const double* __restrict__ id,
+                               double* __restrict__ z, int64_t m, CgState* st, double* partials) {
+    __shared__ double red[32];
+    if (st->done) return;
+    double acc = 0.0;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        const double zk = id ? r[k] * id[k] : r[k];
+        z[k] = zk;
+        acc += r[k] * zk;
+    }
+    double tot;
+    if (!grid_sum_last(acc, partials, &st->ticket[1], red, tot)) return;
+    if (threadIdx.x == 0) {
+        st->beta = st->it == 0 ? 0.0 : (tot - st->rzo) / st->rz;
+        st->rz = tot;
+    }
+}
+
+// p = z + beta p (blas.hpp:50-56). First node of every loop iteration: it is
+// also where a finished solve stops the device-side while loop.
+template <class Z>
+__global__ void k_xpby(const Z* __restrict__ z, double* __restrict__ p, int64_t m, CgState* st) {
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) stop_loop(st);
+        return;
+    }
+    const double beta = st->beta;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) p[k] = (double)z[k] + beta * p[k];
+}
+
+// ap = A p and p . Ap, then alpha or a breakdown (solver.hpp:147-156).
+__global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __restrict__ ap, CgState* st,
+                            double* partials) {
+    __shared__ double red[32];
+    if (st->done) return;
+    const int n = L.n;
+    const int64_t m = (int64_t)n * n;
+    double acc = 0.0;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double y = apply_cell(L, p, i, j);
+        ap[k] = y;
+        acc += p[k] * y;
+    }
+    double pap;
+    if (!grid_sum_last(acc, partials, &st->ticket[2], red, pap)) return;
+    if (threadIdx.x == 0) {
+        if (!(fabs(pap) > 0.0) || !isfinite(pap)) {
+            st->converged = 0;
+            st->done = 1;
+            stop_loop(st);
+        } else {
+            st->alpha = st->rz / pap;
+        }
+    }
+}
+
+// u += alpha p, r -= alpha Ap, ||r||^2 (blas.hpp:62-77), then the stopping
+// test (solver.hpp:159-165). The mixed form also emits r in FP32 as the
+// level-0 right-hand side of the cycle, and r_new . z_old for the flexible
+// (Polak-Ribiere) beta: its FP32 cycle is a slightly inexact preconditioner,
+// and beta = r_new.(z_new - z_old) / r_old.z_old keeps CG's convergence rate
+// with it. For an exact preconditioner r_new . z_old = 0 and the two betas agree.
+__global__ void k_cg_update(const double* __restrict__ p, const double* __restrict__ ap, double* __restrict__ u,
+                            double* __restrict__ r, float* __restrict__ b0f, const float* __restrict__ zold,
+                            int64_t m, CgState* st, double* partials) {
+    __shared__ double red[32];
+    if (st->done) return;
+    const double alpha = st->alpha;
+    double acc = 0.0, acc2 = 0.0;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        u[k] += alpha * p[k];
+        const double rk = r[k] - alpha * ap[k];
+        r[k] = rk;
+        if (b0f) b0f[k] = (float)rk;
+        if (zold) acc2 += rk * (double)zold[k];
+        acc += rk * rk;
+    }
+    double rr, rzo;
+    if (!grid_sum2_last(acc, acc2, partials, &st->ticket[3], red, rr, rzo)) return;
+    if (threadIdx.x == 0) {
+        st->rzo = zold ? rzo : 0.0;
+        const double res = sqrt(rr) / st->bnorm;
+        const int it = st->it + 1;
+        st->residual = res;
+        st->it = it;
+        if (st->record_history && st->history) st->history[it] = res;
+        if (res < st->tol) {
+            st->converged = 1;
+            st->done = 1;
+        } else if (it >= st->max_iter) {
+            st->done = 1;
+        }
+        if (st->done) stop_loop(st);
+    }
+}
+
+// ||b - A u|| / ||b|| from scratch: the honest residual check. Also zeroes u
+// when ||b|| == 0 (f == 0 returns u == 0 whatever the warm start).
+__global__ void k_true_residual(Lvl64 L, double* __restrict__ u, const double* __restrict__ b, CgState* st,
+                                double* partials) {
+    __shared__ double red[32];
+    const int n = L.n;
+    const int64_t m = (int64_t)n * n;
+    const bool zero_u = st->bnorm == 0.0;
+    double acc = 0.0;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        if (zero_u) {
+            u[k] = 0.0;
+            continue;
+        }
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double rk = b[k] - apply_cell(L, u, i, j);
+        acc += rk * rk;
+    }
+    double tot;
+    if (!grid_sum_last(acc, partials, &st->ticket[0], red, tot)) return;
+    if (threadIdx.x == 0) st->true_residual = st->bnorm > 0.0 ? sqrt(tot) / st->bnorm : 0.0;
+}
+
+__global__ void k_apply(Lvl64 L, const double* __restrict__ x, double* __restrict__ y) {
+    const int n = L.n;
+    const int64_t m = (int64_t)n * n;
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        y[k] = apply_cell(L, x, i, j);
+    }
+}
+
+template <class T>
+__global__ void k_copy_cast(const double* __restrict__ src, T* __restrict__ dst, int64_t m) {
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) dst[k] = (T)src[k];
+}
+template <class T>
+__global__ void k_copy_back(const T* __restrict__ src, double* __restrict__ dst, int64_t m) {
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) dst[k] = (double)src[k];
+}
+
+// Coarse tail: one CTA runs `top_calls` cycles on levels l0 .. nlev-1.
+template <class T>
+__global__ void k_tail(const Lvl<T>* __restrict__ lv, int l0, int nlev, int pre, int post, int gamma,
+                       int top_calls, const double* id64, const CgState* st) {
+    if (st && st->done) return;
+    block_cycle<T>(lv, l0, nlev, pre, post, gamma, top_calls, id64);
+}
+
+// Dense coarse tail. The levels from l0 down form a fixed linear map
+// b_{l0} -> x_{l0} ("x = 0, then top_calls cycles": multigrid.hpp:116-118 for
+// l0 > 0, multigrid.hpp:88-93 for l0 = 0). Column j is that map applied to the
+// unit vector e_j, computed by one CTA per column with the level vectors in
+// shared memory and the coefficients read from the (FP64) hierarchy. Stored
+// row-major, FP64 and optionally rounded to FP32 for the mixed form.
+__global__ void k_tail_columns(const Lvl64* __restrict__ h, int l0, int nlev, int pre, int post, int gamma,
+                               int top_calls, int N, double* __restrict__ Td, float* __restrict__ Tf) {
+    extern __shared__ double sm_vec[];
+    __shared__ Lvl<double> lv[kMaxLevels];
+    if (threadIdx.x == 0) {
+        double* ptr = sm_vec;
+        for (int l = l0; l < nlev; ++l) {
+            const Lvl64 H = h[l];
+            const int m = H.n * H.n;
+            lv[l] = Lvl<double>{H.n, H.e, H.nf, H.d, H.id, ptr, ptr + m};
+            ptr += 2 * m;
+        }
+    }
+    __syncthreads();
+    const int j = blockIdx.x;
+    double* b = lv[l0].b;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) b[k] = (k == j) ? 1.0 : 0.0;
+    __syncthreads();
+    block_cycle<double>(lv, l0, nlev, pre, post, gamma, top_calls, nullptr);
+    const double* x = lv[l0].x;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        Td[(size_t)i * N + j] = x[i];
+        if (Tf) Tf[(size_t)i * N + j] = (float)x[i];
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// x_{l0} = T b_{l0}: one warp per row, b staged in shared memory.
+template <class T>
+__global__ void k_tail_matvec(const T* __restrict__ M, int N, const T* __restrict__ b, T* __restrict__ x,
+                              const CgState* st) {
+    if (st && st->done) return;
+    extern __shared__ unsigned char sm_raw[];
+    T* bs = reinterpret_cast<T*>(sm_raw);
+    for (int k = threadIdx.x; k < N; k += blockDim.x) bs[k] = b[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int row = warp; row < N; row += nwarps) {
+        const T* Mr = M + (size_t)row * N;
+        T acc = T(0);
+        for (int c = lane; c < N; c += 32) acc += Mr[c] * bs[c];
+        acc = warp_sum_t(acc);
+        if (lane == 0) x[row] = acc;
+    }
+}
+
+// ------------------------------------------------------------ launch wrappers
+
+void launch_cg_init(const double* f, double h2, int64_t m, double* b, double* r, double* u, double* p,
+                    float* b0f, const double* u0, const Lvl64& L0, CgState* st, double* partials,
+                    cudaStream_t s) {
+    k_cg_init<<<grid_for(m), kThreads, 0, s>>>(f, h2, m, b, r, u, p, b0f, u0, L0, st, partials);
+}
+template <class T>
+void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s) {
+    k_gs<T><<<grid_for(colour_count(L.n, colour)), kThreads, 0, s>>>(L, colour, zero, st);
+}
+template <class T>
+void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s) {
+    const int64_t nc = (L.n + 1) / 2;
+    k_residual_restrict<T><<<grid_for(nc * nc), kThreads, 0, s>>>(L, bc, st);
+}
+template <class T>
+void launch_prolong_gs1(const Lvl<T>& L, const T* xc, CgState* st, cudaStream_t s) {
+    k_prolong_gs1<T><<<grid_for(colour_count(L.n, 1)), kThreads, 0, s>>>(L, xc, st);
+}
+template <class T>
+void launch_gs0_dot(const Lvl<T>& L, const double* r, CgState* st, double* partials, cudaStream_t s) {
+    k_gs0_dot<T><<<grid_for(colour_count(L.n, 0)), kThreads, 0, s>>>(L, r, st, partials);
+}
+template <class T>
+void launch_tail(const Lvl<T>* lv_dev, int l0, int nlev, int pre, int post, int gamma, int top_calls,
+                 const double* id64, CgState* st, int threads, cudaStream_t s) {
+    k_tail<T><<<1, threads, 0, s>>>(lv_dev, l0, nlev, pre, post, gamma, top_calls, id64, st);
+}
+void launch_tail_columns(const Lvl64* h_dev, const Lvl64* h_host, int l0, int nlev, int pre, int post, int gamma,
+                         int top_calls, int N, double* Td, float* Tf, cudaStream_t s) {
+    size_t smem = 0;
+    for (int l = l0; l < nlev; ++l) smem += 2 * sizeof(double) * (size_t)h_host[l].n * h_host[l].n;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_tail_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tail_columns<<<N, 256, smem, s>>>(h_dev, l0, nlev, pre, post, gamma, top_calls, N, Td, Tf);
+}
+template <class T>
+void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaStream_t s) {
+    const int threads = 256;
+    int blocks = (N + threads / 32 - 1) / (threads / 32);
+    if (blocks > kMaxBlocks) blocks = kMaxBlocks;
+    k_tail_matvec<T><<<blocks, threads, sizeof(T) * (size_t)N, s>>>(M, N, b, x, st);
+}
+template <class T>
+void launch_dot_rz(const T* z, const double* r, int64_t m, CgState* st, double* partials, cudaStream_t s) {
+    k_dot_rz<T><<<grid_for(m), kThreads, 0, s>>>(z, r, m, st, partials);
+}
+void launch_precond_diag(const double* r, const double* id, double* z, int64_t m, CgState* st,
+                         double* partials, cudaStream_t s) {
+    k_precond_diag<<<grid_for(m), kThreads, 0, s>>>(r, id, z, m, st, partials);
+}
+template <class Z>
+void launch_xpby(const Z* z, double* p, int64_t m, CgState* st, cudaStream_t s) {
+    k_xpby<Z><<<grid_for(m), kThreads, 0, s>>>(z, p, m, st);
+}
+void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, double* partials,
+                      cudaStream_t s) {
+    k_apply_dot<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, p, ap, st, partials);
+}
+void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, const float* zold,
+                      int64_t m, CgState* st, double* partials, cudaStream_t s) {
+    k_cg_update<<<grid_for(m), kThreads, 0, s>>>(p, ap, u, r, b0f, zold, m, st, partials);
+}
+void launch_true_residual(const Lvl64& L, const double* u, const double* b, double*, CgState* st,
+                          double* partials, cudaStream_t s) {
+    k_true_residual<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, const_cast<double*>(u), b, st,
+                                                                      partials);
+}
+void launch_apply(const Lvl64& L, const double* x, double* y, cudaStream_t s) {
+    k_apply<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, x, y);
+}
+template <class T>
+void launch_copy_cast(const double* src, T* dst, int64_t m, cudaStream_t s) {
+    k_copy_cast<T><<<grid_for(m), kThreads, 0, s>>>(src, dst, m);
+}
+template <class T>
+void launch_copy_back(const T* src, double* dst, int64_t m, cudaStream_t s) {
+    k_copy_back<T><<<grid_for(m), kThreads, 0, s>>>(src, dst, m);
+}
+
+// ================================================================ block engine
+
+// Per-CTA arena layout for one side-n problem: FP64 hierarchy (e, nf, d, id
+// per level, wb/sb boundary vectors), the FP32 coefficient copies when the
+// cycle runs in FP32, the per-level iterate/right-hand side, and the five
+// FP64 CG vectors b, r, p, Ap, z. Level 0 of an FP64 cycle works directly on
+// r (right-hand side) and z (iterate). Shared by host sizing and device carving.
+template <class T>
+__host__ __device__ size_t carve(int n, char* base, Lvl64* h, Lvl<T>* lv, double** cg, int* nlev_out) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        char* ptr = base ? base + off : nullptr;
+        off += (bytes + 255) & ~(size_t)255;
+        return ptr;
+    };
+    int sides[kMaxLevels];
+    int nlev = 0;
+    for (int s = n; nlev < kMaxLevels;) {
+        sides[nlev++] = s;
+        if (s <= 1) break;
+        s = (s + 1) / 2;
+    }
+    const bool fp32 = sizeof(T) == 4;
+    const size_t m0 = (size_t)n * n;
+    for (int l = 0; l < nlev; ++l) {
+        const size_t m = (size_t)sides[l] * sides[l];
+        Lvl64 H;
+        H.n = sides[l];
+        H.e = (double*)take(8 * m);
+        H.nf = (double*)take(8 * m);
+        H.d = (double*)take(8 * m);
+        H.id = (double*)take(8 * m);
+        H.wb = (double*)take(8 * (size_t)sides[l]);
+        H.sb = (double*)take(8 * (size_t)sides[l]);
+        if (h) h[l] = H;
+    }
+    double* v[5];
+    for (int q = 0; q < 5; ++q) v[q] = (double*)take(8 * m0);
+    if (cg)
+        for (int q = 0; q < 5; ++q) cg[q] = v[q];
+    for (int l = 0; l < nlev; ++l) {
+        const size_t m = (size_t)sides[l] * sides[l];
+        Lvl<T> V;
+        V.n = sides[l];
+        if (fp32) {
+            V.e = (const T*)take(4 * m);
+            V.nf = (const T*)take(4 * m);
+            V.d = (const T*)take(4 * m);
+            V.id = (const T*)take(4 * m);
+        } else if (h) {
+            V.e = (const T*)h[l].e;
+            V.nf = (const T*)h[l].nf;
+            V.d = (const T*)h[l].d;
+            V.id = (const T*)h[l].id;
+        }
+        if (l == 0 && !fp32) {
+            V.x = (T*)v[4];  // z
+            V.b = (T*)v[1];  // r
+        } else {
+            V.x = (T*)take(sizeof(T) * m);
+            V.b = (T*)take(sizeof(T) * m);
+        }
+        if (lv) lv[l] = V;
+    }
+    if (nlev_out) *nlev_out = nlev;
+    return off;
+}
+
+int num_levels_for(int n) {
+    int nl = 0;
+    carve<double>(n, nullptr, nullptr, nullptr, nullptr, &nl);
+    return nl;
+}
+
+size_t block_arena_bytes(int n, bool mixed) {
+    return mixed ? carve<float>(n, nullptr, nullptr, nullptr, nullptr, nullptr)
+                 : carve<double>(n, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+// y = A x over a block, FP64, returning sum x . y (or x . x when want_xx).
+__device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* x, double* y, double* red) {
+    const int n = L.n;
+    const int64_t m = (int64_t)n * n;
+    double acc = 0.0;
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double v = apply_cell(L, x, i, j);
+        y[k] = v;
+        acc += x[k] * v;
+    }
+    return block_sum(acc, red);
+}
+
+// z = M r for one problem; returns r . z. For the FP32 cycle, r is rounded
+// into the level-0 right-hand side and the FP32 iterate widened into z.
+template <class T>
+__device__ double block_precondition(const BatchArgs& A, const Lvl64* h, const Lvl<T>* lv, int nlev,
+                                     const double* r, double* z, double* red) {
+    const int n = h[0].n;
+    const int64_t m = (int64_t)n * n;
+    double acc = 0.0;
+    if (A.pc == kPcMultigrid) {
+        if (sizeof(T) == 4) {
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) lv[0].b[k] = (T)r[k];
+            __syncthreads();
+            block_cycle<T>(lv, 0, nlev, A.pre, A.post, A.gamma, 1, h[nlev - 1].id);
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+                const double zk = (double)lv[0].x[k];
+                z[k] = zk;
+                acc += r[k] * zk;
+            }
+        } else {
+            block_cycle<T>(lv, 0, nlev, A.pre, A.post, A.gamma, 1, nullptr);
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) acc += r[k] * z[k];
+        }
+    } else {
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+            const double zk = A.pc == kPcJacobi ? r[k] * h[0].id[k] : r[k];
+            z[k] = zk;
+            acc += r[k] * zk;
+        }
+    }
+    return block_sum(acc, red);
+}
+
+// Build the hierarchy of one problem into the CTA's arena. Returns the first
+// invalid permeability index (~0 if the field is valid).
+template <class T>
+__device__ unsigned long long block_setup(const BatchArgs& A, const double* a, const Lvl64* h, const Lvl<T>* lv,
+                                          int nlev, unsigned long long* s_bad) {
+    if (threadIdx.x == 0) *s_bad = ~0ull;
+    __syncthreads();
+    build_fine<BlockScope>(a, h[0], s_bad);
+    __syncthreads();
+    for (int l = 1; l < nlev; ++l) {
+        coarsen<BlockScope>(h[l - 1], h[l]);
+        __syncthreads();
+    }
+    if (sizeof(T) == 4 && A.pc == kPcMultigrid) {
+        for (int l = 0; l < nlev; ++l)
+            to_fp32<BlockScope>(h[l], (float*)lv[l].e, (float*)lv[l].nf, (float*)lv[l].d, (float*)lv[l].id);
+    }
+    __syncthreads();
+    return *s_bad;
+}
+
+// One whole PCG solve (solver.hpp:83-174) by one CTA.
+template <class T>
+__device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, const Lvl<T>* lv, int nlev,
+                                double* const* cg, double* red, unsigned long long* s_bad) {
+    const int n = A.side[pid];
+    const int64_t m = (int64_t)n * n;
+    const int64_t off = A.off[pid];
+    double* u = A.u + off;
+    double *b = cg[0], *r = cg[1], *p = cg[2], *ap = cg[3], *z = cg[4];
+
+    const unsigned long long bad = block_setup<T>(A, A.a + off, h, lv, nlev, s_bad);
+    if (bad != ~0ull) {
+        if (threadIdx.x == 0) {
+            A.bad[pid] = bad;
+            A.iterations[pid] = 0;
+            A.converged[pid] = 0;
+            A.residual[pid] = 0.0;
+            A.levels[pid] = 1;
+            A.true_residual[pid] = 0.0;
+        }
+        return;
+    }
+
+    const double hh = 1.0 / (double)(n + 1);
+    const double h2 = hh * hh;
+    const double* f = A.f ? (A.f_shared ? A.f : A.f + off) : nullptr;
+    const double* u0 = A.u0 ? A.u0 + off : nullptr;
+    const bool record = A.record_history && A.history && A.count == 1;
+    // FP32 cycle: flexible (Polak-Ribiere) beta, as in the grid engine.
+    const bool flexible = sizeof(T) == 4 && A.pc == kPcMultigrid;
+
+    double sb = 0.0;
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const double bk = (f ? f[k] : A.fscalar) * h2;
+        b[k] = bk;
+        u[k] = u0 ? u0[k] : 0.0;
+        sb += bk * bk;
+    }
+    const double bnorm = sqrt(block_sum(sb, red));
+    int iterations = 0, converged = 0;
+    double residual = 0.0;
+    if (bnorm == 0.0) {
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) u[k] = 0.0;
+        if (threadIdx.x == 0) {
+            A.bad[pid] = ~0ull;
+            A.iterations[pid] = 0;
+            A.converged[pid] = 1;
+            A.residual[pid] = 0.0;
+            A.levels[pid] = 1;
+            A.true_residual[pid] = 0.0;
+        }
+        return;
+    }
+
+    if (u0) {
+        double sr = 0.0;
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+            const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+            const double rk = b[k] - apply_cell(h[0], u, i, j);
+            r[k] = rk;
+            sr += rk * rk;
+        }
+        residual = sqrt(block_sum(sr, red)) / bnorm;
+    } else {
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) r[k] = b[k];
+        residual = 1.0;
+        __syncthreads();
+    }
+    if (record && threadIdx.x == 0) A.history[0] = residual;
+
+    if (residual < A.tol) {
+        converged = 1;
+    } else {
+        double rz = block_precondition<T>(A, h, lv, nlev, r, z, red);
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k];
+        __syncthreads();
+        for (int it = 0; it < A.max_iter; ++it) {
+            const double pap = block_apply_dot(h[0], p, ap, red);
+            if (!(fabs(pap) > 0.0) || !isfinite(pap)) {
+                iterations = it;
+                converged = 0;
+                break;
+            }
+            const double alpha = rz / pap;
+            double rr = 0.0, rzo = 0.0;
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+                u[k] += alpha * p[k];
+                const double rk = r[k] - alpha * ap[k];
+                r[k] = rk;
+                rr += rk * rk;
+                if (flexible) rzo += rk * z[k];  // z still holds the previous direction's z
+            }
+            residual = sqrt(block_sum(rr, red)) / bnorm;
+            if (flexible) rzo = block_sum(rzo, red);
+            iterations = it + 1;
+            if (record && threadIdx.x == 0) A.history[it + 1] = residual;
+            if (residual < A.tol) {
+                converged = 1;
+                break;
+            }
+            const double rz_new = block_precondition<T>(A, h, lv, nlev, r, z, red);
+            const double beta = (rz_new - rzo) / rz;
+            rz = rz_new;
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k] + beta * p[k];
+            __syncthreads();
+        }
+    }
+
+    // Honest residual: ||b - A u|| / ||b|| from scratch.
+    double tr = 0.0;
+    __syncthreads();
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double rk = b[k] - apply_cell(h[0], u, i, j);
+        tr += rk * rk;
+    }
+    const double true_res = sqrt(block_sum(tr, red)) / bnorm;
+    if (threadIdx.x == 0) {
+        A.bad[pid] = ~0ull;
+        A.iterations[pid] = iterations;
+        A.converged[pid] = converged;
+        A.residual[pid] = residual;
+        A.levels[pid] = A.pc == kPcMultigrid ? nlev : 1;
+        A.true_residual[pid] = true_res;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(1024) k_block_solve(BatchArgs A) {
+    __shared__ Lvl64 h[kMaxLevels];
+    __shared__ Lvl<T> lv[kMaxLevels];
+    __shared__ double* cg[5];
+    __shared__ double red[32];
+    __shared__ int s_pid, s_nlev;
+    __shared__ unsigned long long s_bad;
+    char* arena = A.scratch + (size_t)blockIdx.x * A.scratch_stride;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned w = atomicAdd(A.work, 1u);
+            s_pid = w < (unsigned)A.count ? A.order[w] : -1;
+            if (s_pid >= 0) carve<T>(A.side[s_pid], arena, h, lv, cg, &s_nlev);
+        }
+        __syncthreads();
+        const int pid = s_pid;
+        if (pid < 0) return;
+        block_solve_one<T>(A, pid, h, lv, s_nlev, cg, red, &s_bad);
+        __syncthreads();
+    }
+}
+
+// apply_preconditioner hook: hierarchy of problem 0, then z = M r once.
+template <class T>
+__global__ void __launch_bounds__(1024) k_block_precondition(BatchArgs A, const double* r, double* z) {
+    __shared__ Lvl64 h[kMaxLevels];
+    __shared__ Lvl<T> lv[kMaxLevels];
+    __shared__ double* cg[5];
+    __shared__ double red[32];
+    __shared__ int s_nlev;
+    __shared__ unsigned long long s_bad;
+    if (threadIdx.x == 0) carve<T>(A.side[0], A.scratch, h, lv, cg, &s_nlev);
+    __syncthreads();
+    const unsigned long long bad = block_setup<T>(A, A.a, h, lv, s_nlev, &s_bad);
+    if (threadIdx.x == 0) A.bad[0] = bad;
+    if (bad != ~0ull) return;
+    const int64_t m = (int64_t)A.side[0] * A.side[0];
+    double* rr = cg[1];
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) rr[k] = r[k];
+    __syncthreads();
+    block_precondition<T>(A, h, lv, s_nlev, rr, cg[4], red);
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) z[k] = cg[4][k];
+}
+
+template <class T>
+void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream_t s) {
+    k_block_solve<T><<<ctas, threads, 0, s>>>(args);
+}
+template <class T>
+void launch_block_precondition(const BatchArgs& args, const double* r, double* z, int threads, cudaStream_t s) {
+    k_block_precondition<T><<<1, threads, 0, s>>>(args, r, z);
+}
+
+// ------------------------------------------------------ explicit instantiation
+
+#define DGPU_INSTANTIATE(T)                                                                                \
+    template void launch_gs<T>(const Lvl<T>&, int, bool, CgState*, cudaStream_t);                          \
+    template void launch_residual_restrict<T>(const Lvl<T>&, T*, CgState*, cudaStream_t);                  \
+    template void launch_prolong_gs1<T>(const Lvl<T>&, const T*, CgState*, cudaStream_t);                  \
+    template void launch_gs0_dot<T>(const Lvl<T>&, const double*, CgState*, double*, cudaStream_t);        \
+    template void launch_tail<T>(const Lvl<T>*, int, int, int, int, int, int, const double*, CgState*, int, \
+                                 cudaStream_t);                                                            \
+    template void launch_dot_rz<T>(const T*, const double*, int64_t, CgState*, double*, cudaStream_t);     \
+    template void launch_tail_matvec<T>(const T*, int, const T*, T*, CgState*, cudaStream_t);              \
+    template void launch_xpby<T>(const T*, double*, int64_t, CgState*, cudaStream_t);                      \
+    template void launch_copy_cast<T>(const double*, T*, int64_t, cudaStream_t);                           \
+    template void launch_copy_back<T>(const T*, double*, int64_t, cudaStream_t);                           \
+    template void launch_block_solve<T>(const BatchArgs&, int, int, cudaStream_t);                          \
+    template void launch_block_precondition<T>(const BatchArgs&, const double*, double*, int, cudaStream_t);
+
+DGPU_INSTANTIATE(double)
+DGPU_INSTANTIATE(float)
+
+}  // namespace dgpu

@@ -1,0 +1,94 @@
+// Hierarchy construction on the device, always in FP64 (the Galerkin sums
+// and the reciprocal diagonal are the steps whose accuracy the cycle rests on).
+#pragma once
+
+#include <math.h>
+
+#include "common.cuh"
+
+namespace dgpu {
+
+// FP64 level storage, plus the boundary west/south faces used only here.
+struct Lvl64 {
+    int n;
+    double* e;
+    double* nf;
+    double* d;
+    double* id;
+    double* wb;  // west boundary face of row i (cell (i, 0))
+    double* sb;  // south boundary face of column j (cell (0, j))
+};
+
+// include/darcy/level.hpp:57. 2*x*y is (2x)*y: exact scaling then one rounded
+// product, so harmonic(x, y) == harmonic(y, x) bit for bit.
+__device__ __forceinline__ double harmonic(double x, double y) { return 2.0 * x * y / (x + y); }
+
+// level.hpp:79-97 plus validate_permeability (solver.hpp:68-77): the first
+// offending flat index is folded into *bad with atomicMin.
+template <class S>
+__device__ __forceinline__ void build_fine(const double* __restrict__ a, const Lvl64& L,
+                                           unsigned long long* bad) {
+    const int n = L.n;
+    const int64_t m = (int64_t)n * n;
+    for (int64_t k = S::start(); k < m; k += S::stride()) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double c = a[k];
+        if (!(c > 0.0) || !isfinite(c)) atomicMin(bad, (unsigned long long)k);
+        const double e = (j + 1 < n) ? harmonic(c, a[k + 1]) : c;
+        const double w = (j > 0) ? harmonic(c, a[k - 1]) : c;
+        const double nn = (i + 1 < n) ? harmonic(c, a[k + n]) : c;
+        const double s = (i > 0) ? harmonic(c, a[k - n]) : c;
+        const double dd = e + w + nn + s;
+        L.e[k] = e;
+        L.nf[k] = nn;
+        L.d[k] = dd;
+        L.id[k] = 1.0 / dd;
+        if (j == 0) L.wb[i] = w;
+        if (i == 0) L.sb[j] = s;
+    }
+}
+
+// Galerkin coarse operator P^T A P by face summation (level.hpp:171-211),
+// including the width-one trailing aggregate of an odd grid. West/south fine
+// faces come from the neighbour's east/north face (same bits) or, on the
+// domain boundary, from wb/sb; summation order is the reference's.
+template <class S>
+__device__ __forceinline__ void coarsen(const Lvl64& F, const Lvl64& C) {
+    const int n = F.n, nc = C.n;
+    const int64_t mc = (int64_t)nc * nc;
+    for (int64_t K = S::start(); K < mc; K += S::stride()) {
+        const int I = (int)(K / nc), J = (int)(K - (int64_t)I * nc);
+        const int i0 = 2 * I, i1 = (2 * I + 1 < n) ? 2 * I + 1 : 2 * I;
+        const int j0 = 2 * J, j1 = (2 * J + 1 < n) ? 2 * J + 1 : 2 * J;
+        double ce = 0.0, cw = 0.0, cn = 0.0, cs = 0.0;
+        for (int i = i0; i <= i1; ++i) {
+            ce += F.e[(int64_t)i * n + j1];
+            cw += (j0 > 0) ? F.e[(int64_t)i * n + j0 - 1] : F.wb[i];
+        }
+        for (int j = j0; j <= j1; ++j) {
+            cn += F.nf[(int64_t)i1 * n + j];
+            cs += (i0 > 0) ? F.nf[(int64_t)(i0 - 1) * n + j] : F.sb[j];
+        }
+        const double dd = ce + cw + cn + cs;
+        C.e[K] = ce;
+        C.nf[K] = cn;
+        C.d[K] = dd;
+        C.id[K] = 1.0 / dd;
+        if (J == 0) C.wb[I] = cw;
+        if (I == 0) C.sb[J] = cs;
+    }
+}
+
+// FP32 copy of a level's coefficients for the mixed-precision cycle.
+template <class S>
+__device__ __forceinline__ void to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id) {
+    const int64_t m = (int64_t)L.n * L.n;
+    for (int64_t k = S::start(); k < m; k += S::stride()) {
+        e[k] = (float)L.e[k];
+        nf[k] = (float)L.nf[k];
+        d[k] = (float)L.d[k];
+        id[k] = (float)L.id[k];
+    }
+}
+
+}  // namespace dgpu

@@ -1,0 +1,1188 @@
+// Host orchestration and the C ABI (include/darcy_gpu.h).
+//
+// Single large solves go to the grid engine: a per-(n, options) plan owns the
+// device buffers and one CUDA graph holding the whole solve -- hierarchy
+// setup, CG init, first preconditioning, a device-side while loop over CG
+// iterations (conditional graph node), and the honest-residual check -- so a
+// solve is H2D copies, one graph launch, D2H copies. Small and batched solves
+// go to the block engine (one CTA per problem, one launch per batch).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/darcy_gpu.h"
+#include "engine.h"
+
+using namespace dgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Failure {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "CUDA error %s (%s) at solver.cu:%d in %s", cudaGetErrorName(e),
+                  cudaGetErrorString(e), line, what);
+    throw Failure{e == cudaErrorMemoryAllocation ? DGPU_NO_MEMORY : DGPU_CUDA_ERROR, buf};
+}
+#define CK(call)                                          \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) throw_cuda(e_, #call, __LINE__); \
+    } while (0)
+
+[[noreturn]] void invalid(const std::string& msg) { throw Failure{DGPU_INVALID_INPUT, msg}; }
+
+// Grid-engine cut-off: the levels of side <= kTailSide form the coarse tail,
+// applied as one dense matrix (precomputed at setup) per visit.
+constexpr int kTailSide = 32;
+constexpr int kChunk = 8;  // iterations per launch when conditional nodes are unavailable
+
+// Two-pass layout of one device allocation: a pass with base == nullptr only
+// measures, the second carves 256-byte-aligned pieces from a buffer of the
+// measured size. Running the same layout code both times is what keeps the
+// size and the carving from drifting apart.
+struct Carver {
+    char* base = nullptr;
+    size_t cap = 0, off = 0;
+    template <class T>
+    T* take(size_t count) {
+        char* p = base ? base + off : nullptr;
+        off += align_up(count * sizeof(T));
+        if (base && off > cap) throw Failure{DGPU_CUDA_ERROR, "internal layout overflow"};
+        return (T*)p;
+    }
+};
+
+// One owned device allocation.
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0;
+    Arena() = default;
+    Arena(const Arena&) = delete;
+    Arena& operator=(const Arena&) = delete;
+    ~Arena() {
+        if (base) cudaFree(base);
+    }
+    void reserve(size_t bytes) {
+        if (bytes <= size) return;
+        if (base) cudaFree(base);
+        base = nullptr;
+        size = 0;
+        CK(cudaMalloc(&base, bytes));
+        size = bytes;
+    }
+};
+
+template <class T>
+struct DVec {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DVec() {
+        if (p) cudaFree(p);
+    }
+    T* ensure(size_t count) {
+        if (count <= n && p) return p;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        CK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        n = std::max<size_t>(count, 1);
+        return p;
+    }
+};
+
+template <class T>
+struct HVec {  // pinned host staging
+    T* p = nullptr;
+    size_t n = 0;
+    ~HVec() {
+        if (p) cudaFreeHost(p);
+    }
+    T* ensure(size_t count) {
+        if (count <= n && p) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        CK(cudaMallocHost(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        n = std::max<size_t>(count, 1);
+        return p;
+    }
+};
+
+std::vector<int> level_sides(int n) {
+    std::vector<int> s;
+    for (int v = n; (int)s.size() < kMaxLevels;) {
+        s.push_back(v);
+        if (v <= 1) break;
+        v = (v + 1) / 2;
+    }
+    return s;
+}
+
+// ------------------------------------------------------------------ grid plan
+
+struct PlanKey {
+    int n, form, pc, pre, post, gamma, has_f, has_u0;
+    bool operator<(const PlanKey& o) const {
+        return std::tie(n, form, pc, pre, post, gamma, has_f, has_u0) <
+               std::tie(o.n, o.form, o.pc, o.pre, o.post, o.gamma, o.has_f, o.has_u0);
+    }
+};
+
+struct GridPlan {
+    PlanKey key{};
+    int n = 0, nlev = 0, tail_l0 = 0;
+    int ntail = 0;                  // cells of the first tail level (dense operator is ntail x ntail)
+    int64_t m = 0;
+    bool mixed_mg = false;
+    Arena arena;
+    double *a = nullptr, *f = nullptr, *u0 = nullptr, *u = nullptr;
+    double *b = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr;
+    float *x0f = nullptr, *b0f = nullptr;
+    std::vector<Lvl64> h;
+    std::vector<Lvl<double>> lvd;
+    std::vector<Lvl<float>> lvf;
+    void* lv_dev = nullptr;
+    Lvl64* h_dev = nullptr;
+    double* Td = nullptr;           // dense coarse-tail operator, FP64
+    float* Tf = nullptr;            // same, rounded to FP32 (mixed form)
+    CgState* st = nullptr;
+    double* partials = nullptr;
+    DVec<double> history;
+    HVec<CgState> st_host;
+    bool cond = false;
+    size_t nodes_pro = 0, nodes_body = 0, nodes_epi = 0;  // kernel nodes per graph part
+    cudaGraphConditionalHandle handle = 0;
+    cudaGraphExec_t exec = nullptr;     // whole solve (conditional mode)
+    cudaGraphExec_t ex_pro = nullptr, ex_chunk = nullptr, ex_epi = nullptr;  // chunked mode
+    cudaGraphExec_t ex_pc = nullptr;    // preconditioner only (apply_preconditioner)
+    GridPlan() = default;
+    GridPlan(const GridPlan&) = delete;
+    GridPlan& operator=(const GridPlan&) = delete;
+    ~GridPlan() {
+        for (cudaGraphExec_t g : {exec, ex_pro, ex_chunk, ex_epi, ex_pc})
+            if (g) cudaGraphExecDestroy(g);
+    }
+};
+
+}  // namespace
+
+struct dgpu_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex mu;
+    bool cond_ok = false;
+    int sms = 0;
+    std::string info;
+    std::map<PlanKey, std::unique_ptr<GridPlan>> plans;
+    // block-engine buffers
+    DVec<double> ba, bf, bu0, bu, bres, btrue, bhist;
+    DVec<int> border, bside, biter, bconv, blev;
+    DVec<int64_t> boff;
+    DVec<unsigned long long> bbad;
+    DVec<unsigned> bwork;
+    DVec<char> bscratch;
+    DVec<char> flush;
+    // apply_operator / hierarchy buffers
+    DVec<char> misc;
+    int64_t last_launches = 0;
+};
+
+namespace {
+
+// ------------------------------------------------------------ plan building
+
+void alloc_plan(dgpu_context* C, GridPlan& P) {
+    const PlanKey& K = P.key;
+    P.n = K.n;
+    P.m = (int64_t)K.n * K.n;
+    const std::vector<int> sides = level_sides(K.n);
+    P.nlev = (int)sides.size();
+    P.tail_l0 = P.nlev - 1;
+    for (int l = 0; l < P.nlev; ++l)
+        if (sides[l] <= kTailSide) {
+            P.tail_l0 = l;
+            break;
+        }
+    P.ntail = sides[P.tail_l0] * sides[P.tail_l0];
+    P.mixed_mg = K.form == DGPU_FORM_MIXED && K.pc == kPcMultigrid;
+    const size_t m = (size_t)P.m;
+    P.h.assign(P.nlev, Lvl64{});
+    P.lvd.assign(P.nlev, Lvl<double>{});
+    P.lvf.assign(P.nlev, Lvl<float>{});
+    auto layout = [&](Carver& A) {
+        P.a = A.take<double>(m);
+        P.f = A.take<double>(m);
+        P.u0 = A.take<double>(m);
+        P.u = A.take<double>(m);
+        P.b = A.take<double>(m);
+        P.r = A.take<double>(m);
+        P.p = A.take<double>(m);
+        P.ap = A.take<double>(m);
+        P.z = A.take<double>(m);
+        P.x0f = A.take<float>(m);
+        P.b0f = A.take<float>(m);
+        for (int l = 0; l < P.nlev; ++l) {
+            const size_t ml = (size_t)sides[l] * sides[l];
+            Lvl64& H = P.h[l];
+            H.n = sides[l];
+            H.e = A.take<double>(ml);
+            H.nf = A.take<double>(ml);
+            H.d = A.take<double>(ml);
+            H.id = A.take<double>(ml);
+            H.wb = A.take<double>(sides[l]);
+            H.sb = A.take<double>(sides[l]);
+            Lvl<float>& F = P.lvf[l];
+            F.n = sides[l];
+            F.e = A.take<float>(ml);
+            F.nf = A.take<float>(ml);
+            F.d = A.take<float>(ml);
+            F.id = A.take<float>(ml);
+            Lvl<double>& D = P.lvd[l];
+            D.n = sides[l];
+            D.e = H.e;
+            D.nf = H.nf;
+            D.d = H.d;
+            D.id = H.id;
+            double* xv = A.take<double>(ml);
+            double* bv = A.take<double>(ml);
+            if (l == 0) {
+                D.x = P.z;
+                D.b = P.r;
+                F.x = P.x0f;
+                F.b = P.b0f;
+            } else {
+                D.x = xv;
+                D.b = bv;
+                F.x = (float*)xv;
+                F.b = (float*)bv;
+            }
+        }
+        P.Td = A.take<double>((size_t)P.ntail * P.ntail);
+        P.Tf = A.take<float>((size_t)P.ntail * P.ntail);
+        P.h_dev = A.take<Lvl64>(kMaxLevels);
+        P.lv_dev = A.take<Lvl<double>>(kMaxLevels);
+        P.st = A.take<CgState>(1);
+        P.partials = A.take<double>(2 * kMaxBlocks);
+    };
+    Carver probe;
+    layout(probe);
+    P.arena.reserve(probe.off);
+    Carver real{P.arena.base, P.arena.size, 0};
+    layout(real);
+    CK(cudaMemcpy(P.h_dev, P.h.data(), sizeof(Lvl64) * P.nlev, cudaMemcpyHostToDevice));
+    if (P.mixed_mg)
+        CK(cudaMemcpy(P.lv_dev, P.lvf.data(), sizeof(Lvl<float>) * P.nlev, cudaMemcpyHostToDevice));
+    else
+        CK(cudaMemcpy(P.lv_dev, P.lvd.data(), sizeof(Lvl<double>) * P.nlev, cudaMemcpyHostToDevice));
+    P.st_host.ensure(1);
+    (void)C;
+}
+
+template <class T>
+const std::vector<Lvl<T>>& levels_of(const GridPlan& P);
+template <>
+const std::vector<Lvl<double>>& levels_of<double>(const GridPlan& P) {
+    return P.lvd;
+}
+template <>
+const std::vector<Lvl<float>>& levels_of<float>(const GridPlan& P) {
+    return P.lvf;
+}
+
+template <class T>
+const T* tail_matrix(const GridPlan& P);
+template <>
+const double* tail_matrix<double>(const GridPlan& P) {
+    return P.Td;
+}
+template <>
+const float* tail_matrix<float>(const GridPlan& P) {
+    return P.Tf;
+}
+
+// Host mirror of run_cycle (multigrid.hpp:97-127) for the large levels; the
+// levels from tail_l0 down are one dense matvec per parent visit.
+template <class T>
+void emit_visit(GridPlan& P, int l, bool first, cudaStream_t s) {
+    const auto& lv = levels_of<T>(P);
+    const PlanKey& K = P.key;
+    const Lvl<T>& A = lv[l];
+    for (int q = 0; q < K.pre; ++q) {
+        launch_gs<T>(A, 0, first && q == 0, P.st, s);
+        launch_gs<T>(A, 1, false, P.st, s);
+    }
+    launch_residual_restrict<T>(A, lv[l + 1].b, P.st, s);
+    if (l + 1 >= P.tail_l0) {
+        launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, lv[l + 1].x, P.st, s);
+    } else {
+        for (int g = 0; g < K.gamma; ++g) emit_visit<T>(P, l + 1, g == 0, s);
+    }
+    launch_prolong_gs1<T>(A, lv[l + 1].x, P.st, s);
+    for (int q = 0; q < K.post; ++q) {
+        if (q > 0) launch_gs<T>(A, 1, false, P.st, s);
+        if (l == 0 && q + 1 == K.post)
+            launch_gs0_dot<T>(A, P.r, P.st, P.partials, s);
+        else
+            launch_gs<T>(A, 0, false, P.st, s);
+    }
+}
+
+void emit_setup(GridPlan& P, cudaStream_t s) {
+    launch_build_fine(P.a, P.h[0], &P.st->bad, s);
+    for (int l = 1; l < P.nlev; ++l) launch_coarsen(P.h[l - 1], P.h[l], s);
+    if (P.mixed_mg)
+        for (int l = 0; l < P.nlev; ++l)
+            launch_to_fp32(P.h[l], (float*)P.lvf[l].e, (float*)P.lvf[l].nf, (float*)P.lvf[l].d,
+                           (float*)P.lvf[l].id, s);
+    if (P.key.pc == kPcMultigrid) {
+        // The tail operator is built in FP64 (Galerkin levels and the exact
+        // coarsest solve inside it stay FP64) and rounded once for the mixed form.
+        const int top_calls = P.tail_l0 == 0 ? 1 : P.key.gamma;
+        launch_tail_columns(P.h_dev, P.h.data(), P.tail_l0, P.nlev, P.key.pre, P.key.post, P.key.gamma, top_calls,
+                            P.ntail, P.Td, P.mixed_mg ? P.Tf : nullptr, s);
+    }
+}
+
+void emit_precondition(GridPlan& P, cudaStream_t s) {
+    const PlanKey& K = P.key;
+    if (K.pc == kPcMultigrid) {
+        if (P.tail_l0 == 0) {  // the whole hierarchy is the tail: M is one dense matrix
+            if (P.mixed_mg) {
+                launch_tail_matvec<float>(P.Tf, P.ntail, P.b0f, P.x0f, P.st, s);
+                launch_dot_rz<float>(P.x0f, P.r, P.m, P.st, P.partials, s);
+            } else {
+                launch_tail_matvec<double>(P.Td, P.ntail, P.r, P.z, P.st, s);
+                launch_dot_rz<double>(P.z, P.r, P.m, P.st, P.partials, s);
+            }
+        } else if (P.mixed_mg) {
+            emit_visit<float>(P, 0, true, s);
+        } else {
+            emit_visit<double>(P, 0, true, s);
+        }
+    } else {
+        launch_precond_diag(P.r, K.pc == kPcJacobi ? P.h[0].id : nullptr, P.z, P.m, P.st, P.partials, s);
+    }
+}
+
+void emit_prologue(GridPlan& P, cudaStream_t s) {
+    const double hh = 1.0 / (double)(P.n + 1);
+    emit_setup(P, s);
+    launch_cg_init(P.key.has_f ? P.f : nullptr, hh * hh, P.m, P.b, P.r, P.u, P.p, P.mixed_mg ? P.b0f : nullptr,
+                   P.key.has_u0 ? P.u0 : nullptr, P.h[0], P.st, P.partials, s);
+    emit_precondition(P, s);
+}
+
+void emit_body(GridPlan& P, cudaStream_t s) {
+    if (P.mixed_mg)
+        launch_xpby<float>(P.x0f, P.p, P.m, P.st, s);
+    else
+        launch_xpby<double>(P.z, P.p, P.m, P.st, s);
+    launch_apply_dot(P.h[0], P.p, P.ap, P.st, P.partials, s);
+    launch_cg_update(P.p, P.ap, P.u, P.r, P.mixed_mg ? P.b0f : nullptr, P.mixed_mg ? P.x0f : nullptr, P.m, P.st,
+                     P.partials, s);
+    emit_precondition(P, s);
+}
+
+void emit_epilogue(GridPlan& P, cudaStream_t s) {
+    launch_true_residual(P.h[0], P.u, P.b, nullptr, P.st, P.partials, s);
+}
+
+template <class F>
+cudaGraph_t capture(cudaStream_t s, F&& fn) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+        fn();
+    } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    CK(cudaStreamEndCapture(s, &g));
+    CK(cudaGetLastError());
+    return g;
+}
+
+void build_graphs(dgpu_context* C, GridPlan& P) {
+    cudaStream_t s = C->stream;
+    cudaGraph_t gpro = capture(s, [&] { emit_prologue(P, s); });
+    cudaGraph_t gbody = capture(s, [&] { emit_body(P, s); });
+    cudaGraph_t gepi = capture(s, [&] { emit_epilogue(P, s); });
+    CK(cudaGraphGetNodes(gpro, nullptr, &P.nodes_pro));
+    CK(cudaGraphGetNodes(gbody, nullptr, &P.nodes_body));
+    CK(cudaGraphGetNodes(gepi, nullptr, &P.nodes_epi));
+    P.cond = false;
+    if (C->cond_ok) {
+        cudaGraph_t G = nullptr;
+        CK(cudaGraphCreate(&G, 0));
+        cudaGraphNode_t npro, nwhile, nepi;
+        CK(cudaGraphAddChildGraphNode(&npro, G, nullptr, 0, gpro));
+        CK(cudaGraphConditionalHandleCreate(&P.handle, G, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = P.handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        CK(cudaGraphAddNode(&nwhile, G, &npro, nullptr, 1, &cp));
+        // The loop body is captured straight into the conditional node's body
+        // graph, so the kernels that end the loop (cudaGraphSetConditional in
+        // k_xpby / k_apply_dot / k_cg_update) are direct nodes of that body.
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CK(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        emit_body(P, s);
+        CK(cudaStreamEndCapture(s, &body));
+        CK(cudaGetLastError());
+        CK(cudaGraphAddChildGraphNode(&nepi, G, &nwhile, 1, gepi));
+        CK(cudaGraphInstantiate(&P.exec, G, 0));
+        cudaGraphDestroy(G);
+        P.cond = true;
+    } else {
+        cudaGraph_t chunk = nullptr;
+        CK(cudaGraphCreate(&chunk, 0));
+        cudaGraphNode_t prev = nullptr;
+        for (int q = 0; q < kChunk; ++q) {
+            cudaGraphNode_t nd;
+            CK(cudaGraphAddChildGraphNode(&nd, chunk, prev ? &prev : nullptr, prev ? 1 : 0, gbody));
+            prev = nd;
+        }
+        CK(cudaGraphInstantiate(&P.ex_pro, gpro, 0));
+        CK(cudaGraphInstantiate(&P.ex_chunk, chunk, 0));
+        CK(cudaGraphInstantiate(&P.ex_epi, gepi, 0));
+        cudaGraphDestroy(chunk);
+    }
+    cudaGraphDestroy(gpro);
+    cudaGraphDestroy(gbody);
+    cudaGraphDestroy(gepi);
+}
+
+GridPlan& get_plan(dgpu_context* C, const PlanKey& K) {
+    auto it = C->plans.find(K);
+    if (it != C->plans.end()) return *it->second;
+    // keep the cache bounded: plans hold O(n^2) device memory
+    if (C->plans.size() >= 8) C->plans.clear();
+    auto P = std::make_unique<GridPlan>();
+    P->key = K;
+    alloc_plan(C, *P);
+    build_graphs(C, *P);
+    GridPlan& ref = *P;
+    C->plans.emplace(K, std::move(P));
+    return ref;
+}
+
+// --------------------------------------------------------------- validation
+
+void check_options(int64_t n, const dgpu_options* o) {
+    if (!o) invalid("options must not be NULL");
+    if (n < 1) invalid("grid size must be at least 1");                  // solver.hpp:85
+    if (!(o->tol > 0.0)) invalid("tol must be positive");                  // solver.hpp:86
+    if (o->max_iter < 1) invalid("max_iter must be at least 1");           // solver.hpp:87
+    if (o->preconditioner < 0 || o->preconditioner > 2)
+        invalid("unknown preconditioner; expected one of: multigrid, jacobi, none");
+    if (o->pre_sweeps < 1 || o->post_sweeps < 1)                           // bindings.cpp:43-44
+        invalid("pre_sweeps and post_sweeps must be at least 1");
+    if (o->cycle_index < 1 || o->cycle_index > 2)                          // bindings.cpp:45-46
+        invalid("cycle_index must be 1 (V-cycle) or 2 (W-cycle)");
+    if (o->form != DGPU_FORM_FP64 && o->form != DGPU_FORM_MIXED) invalid("unknown form; expected fp64 or mixed");
+    if (n > 46340) invalid("grid size too large for 32-bit cell rows");
+}
+
+[[noreturn]] void bad_permeability(unsigned long long k) {
+    invalid("permeability must be finite and strictly positive everywhere; offending value at flat index " +
+            std::to_string(k));
+}
+
+// ----------------------------------------------------------------- grid solve
+
+void grid_solve(dgpu_context* C, const double* a, const double* f, double fscalar, int64_t n,
+                const dgpu_options* o, const double* u0, double* u_out, double* history_out, dgpu_stats* stats,
+                bool device_ptrs, cudaStream_t user_stream) {
+    PlanKey K{(int)n, o->form, o->preconditioner, o->pre_sweeps, o->post_sweeps, o->cycle_index, f != nullptr,
+              u0 != nullptr};
+    GridPlan& P = get_plan(C, K);
+    cudaStream_t s = C->stream;
+    const size_t bytes = sizeof(double) * (size_t)P.m;
+    const cudaMemcpyKind in = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind out = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (user_stream) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaEventRecord(e, user_stream));
+        CK(cudaStreamWaitEvent(s, e, 0));
+        cudaEventDestroy(e);
+    }
+    double* hist = nullptr;
+    if (o->record_history) hist = P.history.ensure((size_t)o->max_iter + 1);
+    CgState& hs = *P.st_host.p;
+    std::memset(&hs, 0, sizeof hs);
+    hs.tol = o->tol;
+    hs.fscalar = fscalar;
+    hs.max_iter = o->max_iter;
+    hs.record_history = o->record_history ? 1 : 0;
+    hs.history = hist;
+    hs.use_cond = P.cond ? 1 : 0;
+    hs.cond = P.handle;
+    hs.bad = ~0ull;
+    CK(cudaEventRecord(C->ev0, s));
+    CK(cudaMemcpyAsync(P.a, a, bytes, in, s));
+    if (f) CK(cudaMemcpyAsync(P.f, f, bytes, in, s));
+    if (u0) CK(cudaMemcpyAsync(P.u0, u0, bytes, in, s));
+    CK(cudaMemcpyAsync(P.st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
+    if (P.cond) {
+        CK(cudaGraphLaunch(P.exec, s));
+    } else {
+        CK(cudaGraphLaunch(P.ex_pro, s));
+        for (int done = 0; !done;) {
+            CK(cudaGraphLaunch(P.ex_chunk, s));
+            CK(cudaMemcpyAsync(&hs, P.st, sizeof hs, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            done = hs.done;
+        }
+        CK(cudaGraphLaunch(P.ex_epi, s));
+    }
+    CK(cudaMemcpyAsync(u_out, P.u, bytes, out, s));
+    CK(cudaMemcpyAsync(&hs, P.st, sizeof hs, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(C->ev1, s));
+    if (user_stream) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaEventRecord(e, s));
+        CK(cudaStreamWaitEvent(user_stream, e, 0));
+        cudaEventDestroy(e);
+    }
+    CK(cudaStreamSynchronize(s));
+    if (hs.bad != ~0ull) bad_permeability(hs.bad);
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, C->ev0, C->ev1));
+    const bool f_zero = hs.bnorm == 0.0;
+    if (stats) {
+        stats->iterations = hs.it;
+        stats->residual = hs.residual;
+        stats->converged = hs.converged;
+        stats->levels = (o->preconditioner == kPcMultigrid && !f_zero) ? P.nlev : 1;
+        stats->history_len = o->record_history ? hs.it + 1 : 0;
+        stats->true_residual = hs.true_residual;
+        stats->device_ms = ms;
+        // the loop body runs once per iteration, and once more (all early
+        // exits) when the solve was already finished before the first one
+        const int64_t bodies = std::max(hs.it, 1);
+        stats->kernel_launches = (int64_t)P.nodes_pro + bodies * (int64_t)P.nodes_body + (int64_t)P.nodes_epi;
+    }
+    if (history_out && o->record_history)
+        CK(cudaMemcpy(history_out, hist, sizeof(double) * ((size_t)hs.it + 1), cudaMemcpyDeviceToHost));
+}
+
+// --------------------------------------------------------------- block solves
+
+struct BatchOut {
+    int* iterations;
+    double* residuals;
+    int* converged;
+    int* levels;
+    double* true_residual;
+    double* history;
+};
+
+int threads_for_side(int side) {
+    const int64_t cells = (int64_t)side * side;
+    int t = 64;
+    while (t < 512 && t * 8 < cells) t *= 2;
+    return t;
+}
+
+// Packed problems through the block engine. sides/off on the host; a, f, u0
+// host (or device when device_ptrs) packed arrays.
+void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, const std::vector<int64_t>& off,
+                 const double* a, const double* f, int f_shared, double fscalar, const double* u0,
+                 const dgpu_options* o, double* u_out, BatchOut out, bool device_ptrs, float* ms_out) {
+    cudaStream_t s = C->stream;
+    const int64_t total = off[count - 1] + (int64_t)sides[count - 1] * sides[count - 1];
+    const int maxside = *std::max_element(sides.begin(), sides.end());
+    const bool mixed = o->form == DGPU_FORM_MIXED && o->preconditioner == kPcMultigrid;
+    const cudaMemcpyKind in = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind outk = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+
+    std::vector<int> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sides[x] > sides[y]; });
+
+    const int threads = threads_for_side(maxside);
+    const int per_sm = std::max(1, std::min(2048 / threads, 8));
+    const int ctas = (int)std::min<int64_t>(count, (int64_t)C->sms * per_sm);
+    const size_t stride = align_up(block_arena_bytes(maxside, mixed));
+
+    BatchArgs A{};
+    A.count = (int)count;
+    A.a = C->ba.ensure(total);
+    A.u = C->bu.ensure(total);
+    A.f = nullptr;
+    if (f) A.f = C->bf.ensure(f_shared ? (size_t)sides[0] * sides[0] : (size_t)total);
+    A.f_shared = f_shared;
+    A.fscalar = fscalar;
+    A.u0 = u0 ? C->bu0.ensure(total) : nullptr;
+    A.order = C->border.ensure(count);
+    A.side = C->bside.ensure(count);
+    A.off = C->boff.ensure(count);
+    A.iterations = C->biter.ensure(count);
+    A.residual = C->bres.ensure(count);
+    A.converged = C->bconv.ensure(count);
+    A.levels = C->blev.ensure(count);
+    A.true_residual = C->btrue.ensure(count);
+    A.bad = C->bbad.ensure(count);
+    A.work = C->bwork.ensure(1);
+    A.history = (o->record_history && count == 1) ? C->bhist.ensure((size_t)o->max_iter + 1) : nullptr;
+    A.record_history = o->record_history;
+    A.scratch = C->bscratch.ensure(stride * ctas);
+    A.scratch_stride = stride;
+    A.tol = o->tol;
+    A.max_iter = o->max_iter;
+    A.pc = o->preconditioner;
+    A.pre = o->pre_sweeps;
+    A.post = o->post_sweeps;
+    A.gamma = o->cycle_index;
+
+    CK(cudaEventRecord(C->ev0, s));
+    CK(cudaMemcpyAsync((void*)A.a, a, sizeof(double) * total, in, s));
+    if (f)
+        CK(cudaMemcpyAsync((void*)A.f, f, sizeof(double) * (f_shared ? (size_t)sides[0] * sides[0] : (size_t)total),
+                           in, s));
+    if (u0) CK(cudaMemcpyAsync((void*)A.u0, u0, sizeof(double) * total, in, s));
+    CK(cudaMemcpyAsync((void*)A.order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)A.side, sides.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync((void*)A.off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(A.work, 0, sizeof(unsigned), s));
+    if (mixed)
+        launch_block_solve<float>(A, ctas, threads, s);
+    else
+        launch_block_solve<double>(A, ctas, threads, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(u_out, A.u, sizeof(double) * total, outk, s));
+    std::vector<unsigned long long> bad(count);
+    CK(cudaMemcpyAsync(bad.data(), A.bad, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out.iterations, A.iterations, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out.residuals, A.residual, sizeof(double) * count, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out.converged, A.converged, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+    if (out.levels) CK(cudaMemcpyAsync(out.levels, A.levels, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+    if (out.true_residual)
+        CK(cudaMemcpyAsync(out.true_residual, A.true_residual, sizeof(double) * count, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(C->ev1, s));
+    CK(cudaStreamSynchronize(s));
+    for (int64_t q = 0; q < count; ++q)
+        if (bad[q] != ~0ull) bad_permeability(bad[q]);
+    if (out.history && A.history && o->record_history) {
+        const int len = out.iterations[0] + 1;
+        CK(cudaMemcpy(out.history, A.history, sizeof(double) * len, cudaMemcpyDeviceToHost));
+    }
+    if (ms_out) CK(cudaEventElapsedTime(ms_out, C->ev0, C->ev1));
+    C->last_launches = 1;
+}
+
+}  // namespace
+
+// ======================================================================= C ABI
+
+namespace {
+__global__ void k_set_cond(cudaGraphConditionalHandle h, unsigned v) { cudaGraphSetConditional(h, v); }
+__global__ void k_write(int* p, int v) { *p = v; }
+
+// Self-test of device-set graph conditionals with an IF node (no loop, so a
+// runtime that ignored the device call could not hang): the body must run
+// exactly when the device set the condition to 1.
+bool conditional_nodes_work(cudaStream_t s) {
+    int* flag = nullptr;
+    if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return false;
+    bool ok = true;
+    for (unsigned v : {0u, 1u}) {
+        cudaGraph_t G = nullptr;
+        cudaGraphExec_t X = nullptr;
+        int host = -1;
+        bool step_ok = false;
+        do {
+            if (cudaGraphCreate(&G, 0) != cudaSuccess) break;
+            cudaGraphConditionalHandle h;
+            if (cudaGraphConditionalHandleCreate(&h, G, 0, cudaGraphCondAssignDefault) != cudaSuccess) break;
+            cudaGraphNode_t nset, nif, nw;
+            cudaKernelNodeParams kp{};
+            void* args1[] = {&h, &v};
+            kp.func = (void*)k_set_cond;
+            kp.gridDim = dim3(1);
+            kp.blockDim = dim3(1);
+            kp.kernelParams = args1;
+            if (cudaGraphAddKernelNode(&nset, G, nullptr, 0, &kp) != cudaSuccess) break;
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            if (cudaGraphAddNode(&nif, G, &nset, nullptr, 1, &cp) != cudaSuccess) break;
+            int val = 7;
+            void* args2[] = {&flag, &val};
+            cudaKernelNodeParams kw{};
+            kw.func = (void*)k_write;
+            kw.gridDim = dim3(1);
+            kw.blockDim = dim3(1);
+            kw.kernelParams = args2;
+            if (cudaGraphAddKernelNode(&nw, cp.conditional.phGraph_out[0], nullptr, 0, &kw) != cudaSuccess) break;
+            if (cudaGraphInstantiate(&X, G, 0) != cudaSuccess) break;
+            if (cudaMemsetAsync(flag, 0, sizeof(int), s) != cudaSuccess) break;
+            if (cudaGraphLaunch(X, s) != cudaSuccess) break;
+            if (cudaMemcpyAsync(&host, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) break;
+            if (cudaStreamSynchronize(s) != cudaSuccess) break;
+            step_ok = (v == 1) ? host == 7 : host == 0;
+        } while (0);
+        if (X) cudaGraphExecDestroy(X);
+        if (G) cudaGraphDestroy(G);
+        ok = ok && step_ok;
+    }
+    cudaFree(flag);
+    cudaGetLastError();
+    return ok;
+}
+
+int run(const std::function<void()>& fn) {
+    try {
+        fn();
+        g_err.clear();
+        return DGPU_OK;
+    } catch (const Failure& e) {
+        g_err = e.msg;
+        return e.code;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return DGPU_CUDA_ERROR;
+    }
+}
+
+std::vector<int64_t> offsets_of(const std::vector<int>& sides) {
+    std::vector<int64_t> off(sides.size());
+    int64_t acc = 0;
+    for (size_t q = 0; q < sides.size(); ++q) {
+        off[q] = acc;
+        acc += (int64_t)sides[q] * sides[q];
+    }
+    return off;
+}
+
+void solve_any(dgpu_context* C, const double* a, const double* f, double fscalar, int64_t n, const dgpu_options* o,
+               const double* u0, double* u_out, double* history_out, dgpu_stats* stats, bool device_ptrs,
+               cudaStream_t user_stream) {
+    check_options(n, o);
+    if (!a || !u_out) invalid("a and u must not be NULL");
+    std::lock_guard<std::mutex> lock(C->mu);
+    CK(cudaSetDevice(C->device));
+    grid_solve(C, a, f, fscalar, n, o, u0, u_out, history_out, stats, device_ptrs, user_stream);
+}
+
+// z = M r through the grid engine's own preconditioner graph (setup, the
+// large-level kernels and the dense tail): the apply_preconditioner hook
+// therefore checks the exact code path the solves use.
+void grid_precondition(dgpu_context* C, const double* a, const double* r, int64_t n, int pre, int post, int cycle,
+                       int form, double* z) {
+    PlanKey K{(int)n, form, kPcMultigrid, pre, post, cycle, 0, 0};
+    GridPlan& P = get_plan(C, K);
+    cudaStream_t s = C->stream;
+    if (!P.ex_pc) {
+        cudaGraph_t g = capture(s, [&] {
+            emit_setup(P, s);
+            if (P.mixed_mg) launch_copy_cast<float>(P.r, P.b0f, P.m, s);
+            emit_precondition(P, s);
+            if (P.mixed_mg) launch_copy_back<float>(P.x0f, P.z, P.m, s);
+        });
+        CK(cudaGraphInstantiate(&P.ex_pc, g, 0));
+        cudaGraphDestroy(g);
+    }
+    CgState& hs = *P.st_host.p;
+    std::memset(&hs, 0, sizeof hs);
+    hs.bad = ~0ull;
+    hs.max_iter = 1;
+    const size_t bytes = sizeof(double) * (size_t)P.m;
+    CK(cudaMemcpyAsync(P.a, a, bytes, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(P.r, r, bytes, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(P.st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
+    CK(cudaGraphLaunch(P.ex_pc, s));
+    CK(cudaMemcpyAsync(z, P.z, bytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&hs, P.st, sizeof hs, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (hs.bad != ~0ull) bad_permeability(hs.bad);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dgpu_last_error(void) { return g_err.c_str(); }
+
+int dgpu_create(int device, dgpu_context** out) {
+    return run([&] {
+        if (!out) invalid("out must not be NULL");
+        auto C = std::make_unique<dgpu_context>();
+        if (device < 0) CK(cudaGetDevice(&device));
+        C->device = device;
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&C->ev0));
+        CK(cudaEventCreate(&C->ev1));
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, device));
+        C->sms = prop.multiProcessorCount;
+        C->cond_ok = conditional_nodes_work(C->stream);
+        char buf[512];
+        std::snprintf(buf, sizeof buf, "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s",
+                      prop.name, prop.multiProcessorCount, prop.major, prop.minor,
+                      prop.totalGlobalMem / 1073741824.0, prop.l2CacheSize / 1048576.0,
+                      C->cond_ok ? "device-side" : "host-chunked");
+        C->info = buf;
+        *out = C.release();
+    });
+}
+
+void dgpu_destroy(dgpu_context* ctx) {
+    if (!ctx) return;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        cudaSetDevice(ctx->device);
+        ctx->plans.clear();
+        if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+        if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+}
+
+int dgpu_device_info(dgpu_context* ctx, char* out, int capacity) {
+    return run([&] {
+        if (!ctx || !out || capacity < 1) invalid("bad arguments");
+        std::snprintf(out, (size_t)capacity, "%s", ctx->info.c_str());
+    });
+}
+
+int dgpu_num_levels(int64_t n) { return n < 1 ? 0 : num_levels_for((int)std::min<int64_t>(n, 1 << 30)); }
+
+int dgpu_solve(dgpu_context* ctx, const double* a, const double* f, double f_scalar, int64_t n,
+               const dgpu_options* opt, const double* u0, double* u_out, double* history_out, dgpu_stats* stats) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        solve_any(ctx, a, f, f_scalar, n, opt, u0, u_out, history_out, stats, false, nullptr);
+    });
+}
+
+int dgpu_solve_device(dgpu_context* ctx, const double* d_a, const double* d_f, double f_scalar, int64_t n,
+                      const dgpu_options* opt, const double* d_u0, double* d_u, dgpu_stats* stats, void* stream) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        if (opt && opt->record_history) invalid("record_history is not supported on device buffers");
+        solve_any(ctx, d_a, d_f, f_scalar, n, opt, d_u0, d_u, nullptr, stats, true, (cudaStream_t)stream);
+    });
+}
+
+int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double f_scalar, int f_per_sample,
+                     int64_t batch, int64_t n, const dgpu_options* opt, const double* u0, double* u_out,
+                     int* iterations, double* residuals, int* converged, int* levels) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        check_options(n, opt);
+        if (batch < 1) invalid("a must have shape (batch, n, n)");
+        if (!a || !u_out || !iterations || !residuals || !converged) invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        std::vector<int> sides((size_t)batch, (int)n);
+        dgpu_options o = *opt;
+        o.record_history = 0;
+        BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
+        block_solve(ctx, batch, sides, offsets_of(sides), a, f, f_per_sample ? 0 : 1, f_scalar, u0, &o, u_out, bo,
+                    false, nullptr);
+    });
+}
+
+int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, const double* a, const double* f,
+                      double f_scalar, const dgpu_options* opt, const double* u0, double* u_out, int* iterations,
+                      double* residuals, int* converged, int* levels) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        if (count < 1 || !sides) invalid("need at least one problem");
+        std::vector<int> sv((size_t)count);
+        for (int64_t q = 0; q < count; ++q) {
+            check_options(sides[q], opt);
+            sv[q] = (int)sides[q];
+        }
+        if (!a || !u_out || !iterations || !residuals || !converged) invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        dgpu_options o = *opt;
+        o.record_history = 0;
+        BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
+        block_solve(ctx, count, sv, offsets_of(sv), a, f, 0, f_scalar, u0, &o, u_out, bo, false, nullptr);
+    });
+}
+
+int dgpu_apply_operator(dgpu_context* ctx, const double* a, const double* x, int64_t n, double* y) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        if (n < 1) invalid("a must be a square 2-D array with at least one cell");
+        if (!a || !x || !y) invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        cudaStream_t s = ctx->stream;
+        const size_t m = (size_t)n * n;
+        double *da, *dx, *dy;
+        Lvl64 L{};
+        unsigned long long* bad;
+        auto layout = [&](Carver& c) {
+            da = c.take<double>(m);
+            dx = c.take<double>(m);
+            dy = c.take<double>(m);
+            L = Lvl64{(int)n, c.take<double>(m), c.take<double>(m), c.take<double>(m), c.take<double>(m),
+                      c.take<double>((size_t)n), c.take<double>((size_t)n)};
+            bad = c.take<unsigned long long>(1);
+        };
+        Carver probe;
+        layout(probe);
+        Carver real{ctx->misc.ensure(probe.off), probe.off, 0};
+        layout(real);
+        const unsigned long long init = ~0ull;
+        CK(cudaMemcpyAsync(bad, &init, 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(da, a, 8 * m, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dx, x, 8 * m, cudaMemcpyHostToDevice, s));
+        launch_build_fine(da, L, bad, s);
+        launch_apply(L, dx, dy, s);
+        CK(cudaGetLastError());
+        unsigned long long hb = 0;
+        CK(cudaMemcpyAsync(&hb, bad, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(y, dy, 8 * m, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (hb != ~0ull) bad_permeability(hb);
+    });
+}
+
+int dgpu_apply_preconditioner(dgpu_context* ctx, const double* a, const double* r, int64_t n, int pre_sweeps,
+                              int post_sweeps, int cycle_index, int form, double* z) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        if (n < 1) invalid("a must be a square 2-D array with at least one cell");
+        if (!a || !r || !z) invalid("buffers must not be NULL");
+        if (pre_sweeps < 1 || post_sweeps < 1) invalid("sweeps must be at least 1");  // bindings.cpp:235
+        if (cycle_index < 1 || cycle_index > 2) invalid("cycle_index must be 1 or 2");  // bindings.cpp:236
+        if (form != DGPU_FORM_FP64 && form != DGPU_FORM_MIXED) invalid("unknown form; expected fp64 or mixed");
+        if (n > 46340) invalid("grid size too large for 32-bit cell rows");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        grid_precondition(ctx, a, r, n, pre_sweeps, post_sweeps, cycle_index, form, z);
+    });
+}
+
+int64_t dgpu_hierarchy(dgpu_context* ctx, const double* a, int64_t n, double* out, int64_t capacity) {
+    int64_t written = -1;
+    int rc = run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        if (n < 1 || !a || !out) invalid("bad arguments");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        cudaStream_t s = ctx->stream;
+        const std::vector<int> sides = level_sides((int)n);
+        double* da;
+        unsigned long long* bad;
+        std::vector<Lvl64> h(sides.size());
+        auto layout = [&](Carver& c) {
+            da = c.take<double>((size_t)n * n);
+            bad = c.take<unsigned long long>(1);
+            for (size_t l = 0; l < sides.size(); ++l) {
+                const size_t ml = (size_t)sides[l] * sides[l];
+                h[l] = Lvl64{sides[l], c.take<double>(ml), c.take<double>(ml), c.take<double>(ml),
+                             c.take<double>(ml), c.take<double>((size_t)sides[l]), c.take<double>((size_t)sides[l])};
+            }
+        };
+        Carver probe;
+        layout(probe);
+        Carver real{ctx->misc.ensure(probe.off), probe.off, 0};
+        layout(real);
+        const unsigned long long init = ~0ull;
+        CK(cudaMemcpyAsync(bad, &init, 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(da, a, 8 * (size_t)n * n, cudaMemcpyHostToDevice, s));
+        launch_build_fine(da, h[0], bad, s);
+        for (size_t l = 1; l < sides.size(); ++l) launch_coarsen(h[l - 1], h[l], s);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s));
+        int64_t pos = 0;
+        for (size_t l = 0; l < sides.size(); ++l) {
+            const int sd = sides[l];
+            const size_t ml = (size_t)sd * sd;
+            if (pos + 6 * (int64_t)ml > capacity) invalid("capacity too small");
+            std::vector<double> e(ml), nf(ml), d(ml), id(ml), wb(sd), sb(sd);
+            CK(cudaMemcpy(e.data(), h[l].e, 8 * ml, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(nf.data(), h[l].nf, 8 * ml, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(d.data(), h[l].d, 8 * ml, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(id.data(), h[l].id, 8 * ml, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(wb.data(), h[l].wb, 8 * sd, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(sb.data(), h[l].sb, 8 * sd, cudaMemcpyDeviceToHost));
+            double* E = out + pos;
+            double* W = E + ml;
+            double* N = W + ml;
+            double* S = N + ml;
+            double* D = S + ml;
+            double* I = D + ml;
+            for (int i = 0; i < sd; ++i)
+                for (int j = 0; j < sd; ++j) {
+                    const size_t k = (size_t)i * sd + j;
+                    E[k] = e[k];
+                    N[k] = nf[k];
+                    W[k] = j > 0 ? e[k - 1] : wb[i];
+                    S[k] = i > 0 ? nf[k - sd] : sb[j];
+                    D[k] = d[k];
+                    I[k] = id[k];
+                }
+            pos += 6 * (int64_t)ml;
+        }
+        unsigned long long hb = 0;
+        CK(cudaMemcpy(&hb, bad, 8, cudaMemcpyDeviceToHost));
+        if (hb != ~0ull) bad_permeability(hb);
+        written = pos;
+    });
+    return rc == DGPU_OK ? written : -1;
+}
+
+int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dgpu_options* opt, int reps,
+                         dgpu_kernel_time* out, int cap, int* count) {
+    return run([&] {
+        if (!ctx || !a || !out || !count || cap < 1 || reps < 1) invalid("bad arguments");
+        check_options(n, opt);
+        if (opt->preconditioner != kPcMultigrid) invalid("profiling needs the multigrid preconditioner");
+        std::vector<double> u((size_t)(n * n));
+        dgpu_stats st{};
+        dgpu_options o = *opt;
+        o.record_history = 0;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        grid_solve(ctx, a, nullptr, 1.0, n, &o, nullptr, u.data(), nullptr, &st, false, nullptr);
+        PlanKey K{(int)n, o.form, o.preconditioner, o.pre_sweeps, o.post_sweeps, o.cycle_index, 0, 0};
+        GridPlan& P = get_plan(ctx, K);
+        cudaStream_t s = ctx->stream;
+        // A state that never stops: tol 0, no iteration cap, no graph handle.
+        CgState& hs = *P.st_host.p;
+        CK(cudaMemcpy(&hs, P.st, sizeof hs, cudaMemcpyDeviceToHost));
+        hs.done = 0;
+        hs.tol = 0.0;
+        hs.max_iter = 1 << 30;
+        hs.use_cond = 0;
+        hs.record_history = 0;
+        hs.it = 1;
+        for (unsigned& t : hs.ticket) t = 0;
+        const double m = (double)P.m;
+        const bool f32 = P.mixed_mg;
+        const double w = f32 ? 4.0 : 8.0;
+        const int nc = (P.n + 1) / 2;
+        const double mc = (double)nc * nc;
+        int visits_tail = 1;  // tail products per iteration: parent visits = gamma^(tail_l0 - 1)
+        for (int l = 1; l < P.tail_l0; ++l) visits_tail *= K.gamma;
+        struct Item {
+            const char* name;
+            double bytes, per_it;
+            std::function<void()> launch;
+        };
+        std::vector<Item> items;
+        // Lambdas below capture plain pointers and level views only.
+        CgState* const stp = P.st;
+        double* const partials = P.partials;
+        const double* const rvec = P.r;
+        const int ntail = P.ntail;
+        const int64_t mm = P.m;
+        const int tail_l0 = P.tail_l0;
+        auto add_level0 = [&](auto tag) {
+            using T = decltype(tag);
+            const Lvl<T> L0 = levels_of<T>(P)[0];
+            if (tail_l0 == 0) return;
+            const Lvl<T> L1 = levels_of<T>(P)[1];
+            const T* Tm = tail_matrix<T>(P);
+            // algorithmic bytes: every array the kernel must touch, once
+            items.push_back({"gs_colour0_zero(l0)", w * m * 1.5, 1.0, [=] { launch_gs<T>(L0, 0, true, stp, s); }});
+            items.push_back({"gs_colour1(l0)", w * (m * 0.5 * 3 + m * 2 + m), 1.0,
+                             [=] { launch_gs<T>(L0, 1, false, stp, s); }});
+            items.push_back({"residual_restrict(l0)", w * (5 * m + mc), 1.0,
+                             [=] { launch_residual_restrict<T>(L0, L1.b, stp, s); }});
+            items.push_back({"prolong_gs1(l0)", w * (m * 0.5 * 3 + m * 2 + m + mc), 1.0,
+                             [=] { launch_prolong_gs1<T>(L0, L1.x, stp, s); }});
+            items.push_back({"gs0_dot(l0)", w * (m * 0.5 * 3 + m * 2 + m) + 8 * m, 1.0,
+                             [=] { launch_gs0_dot<T>(L0, rvec, stp, partials, s); }});
+            const double nt = (double)ntail;
+            items.push_back({"tail_matvec", w * (nt * nt + 2 * nt), (double)visits_tail,
+                             [=] { launch_tail_matvec<T>(Tm, ntail, L1.b, L1.x, stp, s); }});
+        };
+        if (f32)
+            add_level0(float{});
+        else
+            add_level0(double{});
+        const Lvl64 H0 = P.h[0];
+        double* const pv = P.p;
+        double* const apv = P.ap;
+        double* const uv = P.u;
+        double* const rw = P.r;
+        float* const x0f = P.x0f;
+        float* const b0f = P.b0f;
+        const double* const zv = P.z;
+        if (f32)
+            items.push_back({"xpby", (4 + 16) * m, 1.0, [=] { launch_xpby<float>(x0f, pv, mm, stp, s); }});
+        else
+            items.push_back({"xpby", 24 * m, 1.0, [=] { launch_xpby<double>(zv, pv, mm, stp, s); }});
+        items.push_back({"apply_dot", 40 * m, 1.0, [=] { launch_apply_dot(H0, pv, apv, stp, partials, s); }});
+        items.push_back({"cg_update", (48 + (f32 ? 8 : 0)) * m, 1.0, [=] {
+                             launch_cg_update(pv, apv, uv, rw, f32 ? b0f : nullptr, f32 ? x0f : nullptr, mm, stp,
+                                              partials, s);
+                         }});
+        int q = 0;
+        for (const Item& it : items) {
+            if (q >= cap) break;
+            CK(cudaMemcpyAsync(P.st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
+            cudaGraph_t g = capture(s, [&] {
+                for (int r = 0; r < reps; ++r) it.launch();
+            });
+            cudaGraphExec_t x;
+            CK(cudaGraphInstantiate(&x, g, 0));
+            cudaGraphDestroy(g);
+            CK(cudaGraphLaunch(x, s));  // warm
+            CK(cudaMemcpyAsync(P.st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
+            CK(cudaEventRecord(ctx->ev0, s));
+            CK(cudaGraphLaunch(x, s));
+            CK(cudaEventRecord(ctx->ev1, s));
+            CK(cudaStreamSynchronize(s));
+            cudaGraphExecDestroy(x);
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+            std::snprintf(out[q].name, sizeof out[q].name, "%s", it.name);
+            out[q].avg_ms = ms / reps;
+            out[q].bytes = it.bytes;
+            out[q].launches_per_iteration = it.per_it;
+            ++q;
+        }
+        *count = q;
+    });
+}
+
+int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes) {
+    return run([&] {
+        if (!ctx || bytes < 1) invalid("bad arguments");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        char* p = ctx->flush.ensure((size_t)bytes);
+        CK(cudaMemsetAsync(p, 1, (size_t)bytes, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+}  // extern "C"

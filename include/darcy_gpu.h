@@ -1,0 +1,152 @@
+/*
+ * darcy_gpu.h -- C ABI of the GB300 engine for the darcy MG-PCG solve path.
+ *
+ * libdarcy_gpu.so exports exactly the functions below: plain C types, host
+ * pointers (or, for the *_device variants, device pointers), no C++ or torch
+ * types. It is the layer that sits under the Python extension `_core`
+ * (darcy_cpp_gb300/csrc/bindings.cpp), which keeps the reference's Python
+ * signatures, messages and result types.
+ *
+ * Semantics follow the reference (darcy-cpp v1.0.0):
+ *   - inputs are borrowed and never modified, outputs are written in full;
+ *   - invalid shapes/values/parameters return DGPU_INVALID_INPUT with the
+ *     reference's message text in dgpu_last_error();
+ *   - non-convergence and CG breakdown are NOT errors: stats.converged = 0.
+ *
+ * All entry points are serialised per context (one internal mutex); a context
+ * owns its CUDA stream, device buffers and captured graphs.
+ */
+#ifndef DARCY_GPU_H
+#define DARCY_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define DGPU_OK 0
+#define DGPU_INVALID_INPUT 1 /* reference: darcy::InvalidInput -> ValueError   */
+#define DGPU_CUDA_ERROR 2    /* a CUDA call failed; message in dgpu_last_error */
+#define DGPU_NO_MEMORY 3     /* device allocation failed                       */
+#define DGPU_TIMEOUT 4       /* a bounded device-side wait gave up             */
+
+/* Preconditioners, reference include/darcy/solver.hpp:31-35. */
+#define DGPU_PC_NONE 0
+#define DGPU_PC_JACOBI 1
+#define DGPU_PC_MULTIGRID 2
+
+/* Arithmetic forms. FP64: every step in double, the drop-in for darcy::solve.
+ * MIXED: the multigrid cycle (smoothing, residual, transfers) in FP32 inside
+ * the FP64 CG recurrence; Galerkin assembly, the coarsest solve, dots and the
+ * true residual stay in FP64. */
+#define DGPU_FORM_FP64 0
+#define DGPU_FORM_MIXED 1
+
+typedef struct dgpu_context dgpu_context;
+
+/* reference SolveOptions (solver.hpp:40-46) + MultigridOptions
+ * (multigrid.hpp:29-47) + the arithmetic form. */
+typedef struct {
+    double tol;         /* relative residual ||b - Au|| / ||b||, > 0        */
+    int max_iter;       /* >= 1                                              */
+    int preconditioner; /* DGPU_PC_*                                         */
+    int pre_sweeps;     /* >= 1                                              */
+    int post_sweeps;    /* >= 1                                              */
+    int cycle_index;    /* 1 = V-cycle, 2 = W-cycle                          */
+    int record_history; /* keep the per-iteration relative residual         */
+    int form;           /* DGPU_FORM_*                                       */
+} dgpu_options;
+
+/* reference SolveResult (solver.hpp:48-56) without the arrays. */
+typedef struct {
+    int iterations;
+    double residual;      /* recursive relative residual, as the reference reports */
+    int converged;
+    int levels;           /* multigrid levels (1 without multigrid, or f == 0) */
+    int history_len;      /* entries written to history_out                    */
+    double true_residual; /* ||b - A u|| / ||b|| recomputed on the device     */
+    double device_ms;     /* CUDA-event time of the device work of this call   */
+    int64_t kernel_launches; /* kernels this call launched on the device      */
+} dgpu_stats;
+
+/* One row of dgpu_profile_kernels. */
+typedef struct {
+    char name[48];
+    double avg_ms;           /* mean device time of one launch (CUDA events)   */
+    double bytes;            /* algorithmic bytes one launch moves             */
+    double launches_per_iteration;
+} dgpu_kernel_time;
+
+/* Context lifetime. device < 0 selects the current device. */
+int dgpu_create(int device, dgpu_context** out);
+void dgpu_destroy(dgpu_context* ctx);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* dgpu_last_error(void);
+
+/* Fill `out` (capacity bytes) with "name | SMs | compute capability | ...". */
+int dgpu_device_info(dgpu_context* ctx, char* out, int capacity);
+
+/* darcy::solve, reference solver.hpp:83-174 behind _core.solve
+ * (src/bindings.cpp:117-138). a: n*n permeability; f: n*n forcing or NULL to
+ * use f_scalar everywhere (bindings.cpp:51-63); u0: n*n warm start or NULL
+ * (additive extension); u_out: n*n; history_out: NULL or max_iter + 1. */
+int dgpu_solve(dgpu_context* ctx, const double* a, const double* f, double f_scalar, int64_t n,
+               const dgpu_options* opt, const double* u0, double* u_out, double* history_out,
+               dgpu_stats* stats);
+
+/* Same, on device-resident buffers (no host copies; `stream` may be NULL for
+ * the context's stream, else a cudaStream_t the work is ordered after). */
+int dgpu_solve_device(dgpu_context* ctx, const double* d_a, const double* d_f, double f_scalar, int64_t n,
+                      const dgpu_options* opt, const double* d_u0, double* d_u, dgpu_stats* stats,
+                      void* stream);
+
+/* _core.solve_batch, reference src/bindings.cpp:140-197: `batch` problems of
+ * one side n, packed (batch, n, n). f: NULL (f_scalar), one n*n array shared
+ * by every sample (f_per_sample = 0, the reference's behaviour) or a packed
+ * (batch, n, n) array (f_per_sample = 1). Outputs per sample. levels may be NULL. */
+int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double f_scalar, int f_per_sample,
+                     int64_t batch, int64_t n, const dgpu_options* opt, const double* u0, double* u_out,
+                     int* iterations, double* residuals, int* converged, int* levels);
+
+/* Uneven-size batch (additive extension of solve_batch): problem p has side
+ * sides[p] and occupies cells [off_p, off_p + sides[p]^2) of the packed
+ * arrays, off_p being the running sum. f/u0 follow the same packing or NULL. */
+int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, const double* a,
+                      const double* f, double f_scalar, const dgpu_options* opt, const double* u0,
+                      double* u_out, int* iterations, double* residuals, int* converged, int* levels);
+
+/* _core.apply_operator, reference src/bindings.cpp:199-216: y = A x. */
+int dgpu_apply_operator(dgpu_context* ctx, const double* a, const double* x, int64_t n, double* y);
+
+/* _core.apply_preconditioner, reference src/bindings.cpp:218-245: one cycle
+ * from a zero initial guess, z = M r. */
+int dgpu_apply_preconditioner(dgpu_context* ctx, const double* a, const double* r, int64_t n, int pre_sweeps,
+                              int post_sweeps, int cycle_index, int form, double* z);
+
+/* Hierarchy dump for parity tests (reference level.hpp:79-97, :171-211): per
+ * level l, e, w, n, s, diag, inv_diag (6 * n_l^2 doubles) at the running
+ * offset. Returns the number of doubles written, or -1. */
+int64_t dgpu_hierarchy(dgpu_context* ctx, const double* a, int64_t n, double* out, int64_t capacity);
+
+/* Number of multigrid levels for an n x n grid (multigrid.hpp:55-64). */
+int dgpu_num_levels(int64_t n);
+
+/* Time the kernels of one CG iteration of the grid engine in isolation on
+ * the field `a` (after one full solve): each of the finest-level kernels and
+ * the dense coarse-tail product is launched `reps` times back to back inside a
+ * CUDA graph between CUDA events on the context stream. Writes up to `cap`
+ * rows and their count. Measurement hook; no counterpart in the reference. */
+int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dgpu_options* opt, int reps,
+                         dgpu_kernel_time* out, int cap, int* count);
+
+/* Write `bytes` of device memory on the context stream (evicts L2 between
+ * timed runs). */
+int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

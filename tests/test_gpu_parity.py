@@ -1,0 +1,377 @@
+"""GPU parity: the CUDA path against the CPU oracle and the reference's golden vectors.
+
+Bars (the reference computes in FP64):
+  * hierarchy (harmonic faces, Galerkin face sums, 1/diag): bit-exact -- no
+    multiply-add is fused there, so the GPU reproduces the CPU bits;
+  * operator / smoother / preconditioner: FMA contraction on the GPU, so a
+    relative 1e-12 element-wise bar;
+  * solves: iterations equal to the oracle's (+-1 where a residual lands
+    within rounding of tol), u within 1e-9 relative L2 of the oracle,
+    reported residual < tol and honest (within 25% of ||b - A u|| / ||b||).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import two_phase
+
+pytestmark = pytest.mark.gpu
+
+REL_L2 = 1e-9
+
+
+@pytest.fixture(scope="module")
+def darcy():
+    import darcy_cpp_gb300
+
+    return darcy_cpp_gb300
+
+
+def rel_l2(x, y) -> float:
+    return float(np.linalg.norm(np.asarray(x) - np.asarray(y)) / max(np.linalg.norm(y), 1e-300))
+
+
+def oracle_threads(orc, n):
+    orc.set_threads(min(16, orc.cpu_count()) if n >= 256 else 1)
+
+
+def true_residual(orc, a, u, f=1.0) -> float:
+    """||b - A u|| / ||b|| on the CPU (b = f h^2)."""
+    n = a.shape[0]
+    b = np.broadcast_to(np.asarray(f, dtype=np.float64), (n, n)) * (1.0 / (n + 1)) ** 2
+    return float(np.linalg.norm(b - orc.apply_operator(a, u)) / np.linalg.norm(b))
+
+
+# --------------------------------------------------------------- hierarchy
+
+@pytest.mark.parametrize("n", [1, 2, 3, 13, 64, 65, 100, 257])
+def test_hierarchy_is_bit_exact(darcy, orc, n) -> None:
+    rng = np.random.default_rng(n)
+    a = np.exp(rng.normal(0.0, 2.0, (n, n)))
+    got = darcy._core.hierarchy(a)
+    want = orc.hierarchy(a)
+    off = 0
+    for L in want:
+        m = L["e"].size
+        for q, k in enumerate(("e", "w", "n", "s", "diag", "inv_diag")):
+            g = got[off + q * m: off + (q + 1) * m].reshape(L[k].shape)
+            assert np.array_equal(g, L[k]), (n, k)
+        off += 6 * m
+    assert off == got.size
+
+
+def test_hierarchy_matches_golden(darcy, golden) -> None:
+    arrays, _ = golden
+    a = arrays["a_h13"]
+    got = darcy._core.hierarchy(a)
+    off = 0
+    for lvl, side in enumerate([13, 7, 4, 2, 1]):
+        m = side * side
+        diag = got[off + 4 * m: off + 5 * m].reshape(side, side)
+        inv = got[off + 5 * m: off + 6 * m].reshape(side, side)
+        assert np.array_equal(diag, arrays[f"h13_l{lvl}_diag"])
+        assert np.array_equal(inv, arrays[f"h13_l{lvl}_inv_diag"])
+        off += 6 * m
+
+
+# ---------------------------------------------------------------- operator
+
+def test_apply_operator_matches_golden(darcy, golden) -> None:
+    arrays, _ = golden
+    y = darcy.apply_operator(arrays["a_op17"], arrays["x_op17"])
+    assert np.allclose(y, arrays["y_op17"], rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("n", [1, 5, 64, 300, 1024])
+def test_apply_operator_matches_oracle(darcy, orc, n) -> None:
+    rng = np.random.default_rng(7 + n)
+    a = two_phase(n, seed=n, hi=1e3, lo=1e-3) if n > 5 else np.exp(rng.normal(size=(n, n)))
+    x = rng.standard_normal((n, n))
+    y = darcy.apply_operator(a, x)
+    ref = orc.apply_operator(a, x)
+    scale = np.abs(a).max() * np.abs(x).max() * 4
+    assert np.abs(y - ref).max() <= 1e-14 * scale
+
+
+def test_operator_symmetric_and_positive(darcy) -> None:
+    rng = np.random.default_rng(1)
+    a = two_phase(24, seed=5)
+    for _ in range(5):
+        x, y = rng.standard_normal((24, 24)), rng.standard_normal((24, 24))
+        left = float(np.sum(darcy.apply_operator(a, x) * y))
+        right = float(np.sum(x * darcy.apply_operator(a, y)))
+        assert abs(left - right) <= 1e-10 * max(abs(left), 1.0)
+        assert float(np.sum(x * darcy.apply_operator(a, x))) > 0
+
+
+# ---------------------------------------------------------- preconditioner
+
+@pytest.mark.parametrize("cycle", [1, 2])
+@pytest.mark.parametrize("sweeps", [1, 2, 3])
+def test_apply_preconditioner_matches_golden(darcy, golden, cycle, sweeps) -> None:
+    arrays, _ = golden
+    z = darcy.apply_preconditioner(arrays["a_pc32"], arrays["r_pc32"], pre_sweeps=sweeps, post_sweeps=sweeps,
+                                   cycle_index=cycle)
+    want = arrays[f"z_pc32_c{cycle}_s{sweeps}"]
+    assert rel_l2(z, want) < 1e-12
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 7, 33, 64, 100])
+def test_apply_preconditioner_matches_oracle(darcy, orc, n) -> None:
+    rng = np.random.default_rng(n)
+    a = np.where(rng.random((n, n)) < 0.5, 3.0, 12.0)
+    r = rng.standard_normal((n, n))
+    for cycle in (1, 2):
+        z = darcy.apply_preconditioner(a, r, cycle_index=cycle)
+        assert rel_l2(z, orc.apply_preconditioner(a, r, cycle_index=cycle)) < 1e-12
+
+
+def test_mixed_preconditioner_close_to_fp64(darcy, orc) -> None:
+    rng = np.random.default_rng(3)
+    a = two_phase(64, seed=3)
+    r = rng.standard_normal((64, 64))
+    z = darcy.apply_preconditioner(a, r, form="mixed")
+    assert rel_l2(z, orc.apply_preconditioner(a, r)) < 1e-5
+
+
+@pytest.mark.parametrize("cycle", [1, 2])
+def test_preconditioner_symmetric_positive(darcy, cycle) -> None:
+    rng = np.random.default_rng(4)
+    a = two_phase(32, seed=8)
+    for _ in range(3):
+        r, s = rng.standard_normal((32, 32)), rng.standard_normal((32, 32))
+        mr = darcy.apply_preconditioner(a, r, cycle_index=cycle)
+        ms = darcy.apply_preconditioner(a, s, cycle_index=cycle)
+        left, right = float(np.sum(mr * s)), float(np.sum(ms * r))
+        assert abs(left - right) / max(abs(left), abs(right)) < 1e-10
+        assert float(np.sum(mr * r)) > 0
+
+
+# -------------------------------------------------------------- solves: golden
+
+def test_cfg1_matches_reference(darcy, golden) -> None:
+    """64x64 seed 0 {12,3}: 21 iterations, 7 levels, residual 4.4554e-11."""
+    arrays, meta = golden
+    spec = meta["solves"]["cfg1"]
+    out = darcy.solve(arrays["a_cfg1"], tol=1e-10, record_history=True)
+    assert out.converged and out.levels == spec["levels"] == 7
+    assert out.iterations == spec["iterations"] == 21
+    assert rel_l2(out.u, arrays["u_cfg1"]) < REL_L2
+    assert abs(out.residual - spec["residual"]) <= 0.25 * spec["residual"]
+    assert len(out.history) == out.iterations + 1 and out.history[0] == 1.0
+    assert np.allclose(out.history[:-1], spec["history"][:-1], rtol=1e-6)
+
+
+SMALL = [f"tiny{n}" for n in (1, 2, 3, 4, 5)] + [f"n{n}_{pc}" for n in (16, 17, 31, 32, 33, 48)
+                                                 for pc in ("multigrid", "jacobi", "none")] + [
+    f"n48_c{c}_s{s}" for c in (1, 2) for s in (1, 2, 3)] + ["fvar32", "contrast1e6_64", "table128"]
+
+
+def _field(name, arrays, n):
+    if name.startswith("tiny"):
+        return np.full((n, n), 2.0), 1.0
+    if name == "fvar32":
+        return two_phase(32, 3), arrays["f_var32"]
+    if name == "contrast1e6_64":
+        return two_phase(64, 13, 1e6, 1.0), 1.0
+    if name.startswith("n48_c"):
+        return two_phase(48, 4), 1.0
+    if name.startswith("table"):
+        return two_phase(n, 0), 1.0
+    return two_phase(n, n), 1.0
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_solve_matches_golden(darcy, golden, name) -> None:
+    arrays, meta = golden
+    spec = meta["solves"][name]
+    a, f = _field(name, arrays, spec["n"])
+    out = darcy.solve(a, f, **spec["kwargs"])
+    assert out.levels == spec["levels"]
+    assert out.converged == spec["converged"]
+    slack = 1 if spec["iterations"] < 100 else max(2, spec["iterations"] // 50)
+    assert abs(out.iterations - spec["iterations"]) <= slack, (out.iterations, spec["iterations"])
+    if f"u_{name}" in arrays:
+        assert rel_l2(out.u, arrays[f"u_{name}"]) < REL_L2
+    assert abs(out.u.sum() - spec["u_sum"]) <= REL_L2 * abs(spec["u_sum"]) * 10
+
+
+# --------------------------------------------------------------- grid engine
+
+@pytest.mark.parametrize("n, cycle", [(64, 2), (65, 2), (100, 1), (127, 2), (128, 2), (200, 2), (256, 1),
+                                      (256, 2), (511, 2)])
+def test_grid_engine_matches_oracle(darcy, orc, n, cycle) -> None:
+    a = two_phase(n, seed=n, hi=1e2, lo=1e-2)
+    oracle_threads(orc, n)
+    want = orc.solve(a, tol=1e-10, cycle_index=cycle)
+    orc.set_threads(1)
+    got = darcy.solve(a, tol=1e-10, cycle_index=cycle)
+    assert got.converged and got.levels == want["levels"]
+    assert abs(got.iterations - want["iterations"]) <= 1
+    assert rel_l2(got.u, want["u"]) < REL_L2
+    assert got.residual < 1e-10
+    # The recursive residual drifts from the true one at high contrast (the
+    # reference drifts the same way); the GPU's true residual must match the
+    # oracle's solution quality.
+    assert got.true_residual <= 2.0 * true_residual(orc, a, want["u"]) + 1e-11
+
+
+@pytest.mark.parametrize("pc", ["jacobi", "none"])
+def test_grid_engine_simple_preconditioners(darcy, orc, pc) -> None:
+    a = two_phase(96, seed=2)
+    want = orc.solve(a, tol=1e-10, preconditioner=pc, max_iter=100000)
+    got = darcy.solve(a, tol=1e-10, preconditioner=pc, max_iter=100000)
+    assert got.converged and got.levels == 1
+    assert abs(got.iterations - want["iterations"]) <= max(2, want["iterations"] // 100)
+    assert rel_l2(got.u, want["u"]) < REL_L2
+
+
+def test_cfg2_1024_matches_reference(darcy, orc, golden) -> None:
+    """1024x1024 seed 1, a in {1e3, 1e-3}: 100 iterations, 11 levels."""
+    _, meta = golden
+    spec = meta["solves"]["cfg2_1024"]
+    a = two_phase(1024, seed=1, hi=1e3, lo=1e-3)
+    got = darcy.solve(a, tol=1e-10)
+    assert got.converged and got.levels == 11
+    assert abs(got.iterations - spec["iterations"]) <= 2
+    assert abs(got.u.sum() - spec["u_sum"]) <= 1e-9 * abs(spec["u_sum"])
+    oracle_threads(orc, 1024)
+    want = orc.solve(a, tol=1e-10)
+    orc.set_threads(1)
+    assert rel_l2(got.u, want["u"]) < REL_L2
+
+
+# -------------------------------------------------------------- mixed form
+
+@pytest.mark.parametrize("n, hi, lo", [(64, 12.0, 3.0), (128, 1e2, 1e-2), (256, 12.0, 3.0), (1024, 1e3, 1e-3)])
+def test_mixed_form_error_against_fp64_oracle(darcy, orc, n, hi, lo) -> None:
+    """FP32 cycle inside FP64 CG still reaches 1e-10, within 1e-9 of the FP64 solution."""
+    a = two_phase(n, seed=1, hi=hi, lo=lo)
+    oracle_threads(orc, n)
+    want = orc.solve(a, tol=1e-10)
+    orc.set_threads(1)
+    got = darcy.solve(a, tol=1e-10, form="mixed")
+    assert got.converged and got.residual < 1e-10
+    assert got.true_residual <= 2.0 * true_residual(orc, a, want["u"]) + 1e-11
+    assert got.iterations <= want["iterations"] + max(2, want["iterations"] // 10)
+    assert rel_l2(got.u, want["u"]) < REL_L2
+
+
+# -------------------------------------------------------------- batched
+
+def test_batch_matches_serial_and_oracle(darcy, orc, golden) -> None:
+    arrays, meta = golden
+    batch_a = arrays["batch_a32"]
+    out = darcy.solve_batch(batch_a, tol=1e-12)
+    assert out.all_converged and out.u.shape == batch_a.shape
+    assert list(out.iterations) == meta["batch32_iterations"]
+    for i, a in enumerate(batch_a):
+        assert np.allclose(out.u[i], darcy.solve(a, tol=1e-12).u, atol=1e-13, rtol=0)
+        assert rel_l2(out.u[i], orc.solve(a, tol=1e-12)["u"]) < REL_L2
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_batch_is_deterministic(darcy, form) -> None:
+    batch_a = np.stack([two_phase(48, seed=s) for s in range(8)])
+    first = darcy.solve_batch(batch_a, tol=1e-12, form=form)
+    second = darcy.solve_batch(batch_a, tol=1e-12, form=form, threads=8)
+    assert np.array_equal(first.iterations, second.iterations)
+    assert np.array_equal(first.u, second.u)
+
+
+def test_uneven_batch_matches_oracle(darcy, orc) -> None:
+    sides = [32, 48, 64, 96, 128, 192, 256, 33, 17, 1, 2]
+    fields = [two_phase(s, seed=10 + q) for q, s in enumerate(sides)]
+    for form in ("fp64", "mixed"):
+        out = darcy.solve_batch_uneven(fields, tol=1e-10, form=form)
+        assert out.all_converged
+        for q, a in enumerate(fields):
+            want = orc.solve(a, tol=1e-10)
+            assert out.levels[q] == want["levels"]
+            assert out.u[q].shape == a.shape
+            assert rel_l2(out.u[q], want["u"]) < REL_L2
+            if form == "fp64":
+                assert abs(out.iterations[q] - want["iterations"]) <= 1
+
+
+def test_batch_reports_per_sample_diagnostics(darcy) -> None:
+    batch = darcy.solve_batch(np.stack([two_phase(32, seed=s) for s in range(5)]), max_iter=2)
+    assert not batch.all_converged
+    assert batch.iterations.shape == (5,) and (batch.iterations == 2).all()
+    assert batch.residuals.shape == (5,) and batch.converged.dtype == bool
+
+
+def test_batch_propagates_validation_errors(darcy) -> None:
+    batch_a = np.stack([np.full((8, 8), 2.0) for _ in range(3)])
+    batch_a[1, 0, 0] = -1.0
+    with pytest.raises(ValueError, match="positive"):
+        darcy.solve_batch(batch_a)
+
+
+# ------------------------------------------------------ edge cases / failures
+
+@pytest.mark.parametrize("n", [8, 100])
+@pytest.mark.parametrize("bad", [0.0, -1.0, np.nan, np.inf])
+def test_rejects_invalid_permeability(darcy, n, bad) -> None:
+    a = np.full((n, n), 2.0)
+    a[3, 4] = bad
+    with pytest.raises(ValueError, match=f"positive.*flat index {3 * n + 4}"):
+        darcy.solve(a)
+
+
+@pytest.mark.parametrize("n", [16, 128])
+def test_zero_forcing_short_circuits(darcy, n) -> None:
+    out = darcy.solve(two_phase(n, seed=1), f=0.0)
+    assert out.converged and out.iterations == 0 and out.levels == 1
+    assert np.all(out.u == 0.0)
+
+
+@pytest.mark.parametrize("n", [32, 128])
+def test_non_convergence_is_reported(darcy, n) -> None:
+    out = darcy.solve(two_phase(n, seed=0), tol=1e-14, max_iter=2)
+    assert not out.converged and out.iterations == 2 and out.residual > 1e-14
+    assert np.isfinite(out.u).all()
+
+
+@pytest.mark.parametrize("n", [40, 160])
+def test_warm_start(darcy, orc, n) -> None:
+    a = two_phase(n, seed=3)
+    exact = darcy.solve(a, tol=1e-12).u
+    warm = darcy.solve(a, tol=1e-10, x0=exact)
+    assert warm.converged and warm.iterations == 0
+    cold = darcy.solve(a, tol=1e-10)
+    half = darcy.solve(a, tol=1e-10, x0=0.9 * exact)
+    want = orc.solve(a, tol=1e-10, u0=0.9 * exact)
+    assert half.converged and half.iterations <= cold.iterations
+    assert abs(half.iterations - want["iterations"]) <= 1
+    assert rel_l2(half.u, want["u"]) < REL_L2
+
+
+@pytest.mark.parametrize("n", [24, 96])
+def test_variable_forcing_and_linearity(darcy, orc, n) -> None:
+    a = two_phase(n, seed=4)
+    xs = np.linspace(0, 1, n)
+    f = np.outer(np.sin(np.pi * xs), 1.0 + xs**2)
+    got = darcy.solve(a, f, tol=1e-12)
+    assert rel_l2(got.u, orc.solve(a, f, tol=1e-12)["u"]) < REL_L2
+    u1 = darcy.solve(a, 1.0, tol=1e-13).u
+    u3 = darcy.solve(a, 3.0, tol=1e-13).u
+    assert np.allclose(3.0 * u1, u3, rtol=1e-8)
+
+
+def test_record_history_grid_engine(darcy, orc) -> None:
+    a = two_phase(128, seed=3)
+    got = darcy.solve(a, tol=1e-10, record_history=True)
+    want = orc.solve(a, tol=1e-10, record_history=True)
+    assert len(got.history) == got.iterations + 1 and got.history[0] == 1.0
+    k = min(len(got.history), len(want["history"])) - 1
+    assert np.allclose(got.history[:k], want["history"][:k], rtol=1e-6)
+
+
+def test_repeated_solves_are_deterministic(darcy) -> None:
+    a = two_phase(300, seed=9, hi=1e2, lo=1e-2)
+    first, second = darcy.solve(a), darcy.solve(a)
+    assert first.iterations == second.iterations
+    assert np.array_equal(first.u, second.u)

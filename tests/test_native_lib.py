@@ -1,0 +1,95 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+symbol include/darcy_gpu.h declares, and the extension validates its inputs
+before touching the device (reference src/bindings.cpp:33-78 messages)."""
+
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__
+
+    builder = __graft_entry__._builder()
+    if not builder.LIB.exists() or not builder.EXT.exists():
+        builder.build()
+    return builder.LIB
+
+
+def declared_symbols() -> list[str]:
+    text = (ROOT / "include" / "darcy_gpu.h").read_text()
+    return sorted(set(re.findall(r"\b(dgpu_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_reference_entry_points() -> None:
+    names = declared_symbols()
+    for want in ("dgpu_solve", "dgpu_solve_batch", "dgpu_apply_operator", "dgpu_apply_preconditioner",
+                 "dgpu_last_error", "dgpu_create", "dgpu_destroy"):
+        assert want in names
+
+
+def test_library_exports_every_declared_symbol(built) -> None:
+    lib = ctypes.CDLL(str(built))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_num_levels_without_a_device(built) -> None:
+    lib = ctypes.CDLL(str(built))
+    lib.dgpu_num_levels.argtypes = [ctypes.c_int64]
+    for n, want in [(1, 1), (2, 2), (4, 3), (8, 4), (16, 5), (64, 7), (128, 8), (1024, 11), (2048, 12),
+                    (17, 6), (33, 7), (47, 7), (63, 7)]:
+        assert lib.dgpu_num_levels(n) == want
+
+
+def test_build_info_has_exactly_the_reference_keys(built) -> None:
+    import darcy_cpp_gb300 as darcy
+
+    info = darcy.build_info()
+    assert set(info) == {"version", "compiler", "openmp", "max_threads", "numpy"}
+    assert isinstance(info["openmp"], bool) and info["max_threads"] >= 1
+    assert darcy.__version__.count(".") == 2
+
+
+@pytest.mark.parametrize("call, match", [
+    (lambda d: d.solve(np.ones((4, 8))), "square"),
+    (lambda d: d.solve(np.ones((4, 4, 4))), "square"),
+    (lambda d: d.solve(np.ones((0, 0))), "square"),
+    (lambda d: d.solve(np.ones((8, 8)), np.ones((4, 4))), "same shape"),
+    (lambda d: d.solve(np.ones((8, 8)), preconditioner="ilu"), "unknown preconditioner"),
+    (lambda d: d.solve(np.ones((8, 8)), tol=0.0), "tol"),
+    (lambda d: d.solve(np.ones((8, 8)), tol=-1e-3), "tol"),
+    (lambda d: d.solve(np.ones((8, 8)), max_iter=0), "max_iter"),
+    (lambda d: d.solve(np.ones((8, 8)), pre_sweeps=0), "sweeps"),
+    (lambda d: d.solve(np.ones((8, 8)), post_sweeps=0), "sweeps"),
+    (lambda d: d.solve(np.ones((8, 8)), cycle_index=3), "cycle_index"),
+    (lambda d: d.solve(np.ones((8, 8)), form="fp16"), "unknown form"),
+    (lambda d: d.solve_batch(np.ones((8, 8))), r"batch, n, n"),
+    (lambda d: d.apply_operator(np.ones((8, 8)), np.ones((4, 4))), "same shape"),
+    (lambda d: d.apply_preconditioner(np.ones((8, 8)), np.ones((8, 4))), "square"),
+    (lambda d: d.solve(np.ones((8, 8)), x0=np.ones((4, 4))), "same shape"),
+])
+def test_validation_happens_on_the_host(built, call, match) -> None:
+    import darcy_cpp_gb300 as darcy
+
+    with pytest.raises(ValueError, match=match):
+        call(darcy)
+
+
+def test_fields_are_exported(built) -> None:
+    import darcy_cpp_gb300 as darcy
+
+    a = darcy.two_phase_permeability(darcy.gaussian_random_field(16, seed=1), hi=9.0, lo=2.0)
+    assert set(np.unique(a)) == {2.0, 9.0}
+    with pytest.raises(ValueError, match="positive"):
+        darcy.two_phase_permeability(np.zeros((8, 8)), hi=1.0, lo=-1.0)
+    with pytest.raises(ValueError):
+        darcy.gaussian_random_field(0)
