@@ -52,8 +52,8 @@ __host__ __device__ inline int64_t colour_count(int n, int c) {
 // t-th cell of colour c, in row-major order. Rows pair up: rows 2p and 2p+1
 // together hold exactly n cells of each colour.
 __device__ __forceinline__ void colour_cell(int n, int c, int64_t t, int& i, int& j) {
-    const int64_t p = t / n;
-    const int r = (int)(t - p * n);
+    const int p = (int)t / n;  // cells < 2^31: grids are capped at n = 46340
+    const int r = (int)t - p * n;
     const int o0 = c & 1;
     const int cnt0 = (n - o0 + 1) >> 1;
     if (r < cnt0) {
@@ -145,6 +145,20 @@ __device__ __forceinline__ void prolong_gs1(const Lvl<T> L, const T* xc) {
         if (i > 0) v += L.nf[k - n] * (L.x[k - n] + xc[(int64_t)((i - 1) >> 1) * nc + (j >> 1)]);
         L.x[k] = v * L.id[k];
     }
+}
+
+// ------------------------------------------------- programmatic launches
+//
+// Kernels of a solve graph are launched with programmatic stream
+// serialization: a kernel may be scheduled while its predecessor is still
+// running, waits in pdl_wait() for the predecessor's completion and memory
+// flush, and immediately lets its own successor be scheduled (pdl_trigger).
+// Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() {
+    pdl_wait();
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------ reductions

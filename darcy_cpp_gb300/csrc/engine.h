@@ -58,6 +58,7 @@ struct BatchArgs {
     unsigned* work;             // dynamic work counter (zeroed before launch)
     char* scratch;              // per-CTA arena
     size_t scratch_stride;
+    size_t smem_budget;         // dynamic shared memory per CTA for the coarse levels
     double tol;
     int max_iter;
     int pc;                     // 0 none, 1 jacobi, 2 multigrid
@@ -72,8 +73,13 @@ constexpr int kMaxBlocks = 152 * 8;
 inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Bytes of per-CTA scratch the batched engine needs for a side-n problem.
-size_t block_arena_bytes(int n, bool mixed);
+size_t block_arena_bytes(int n, bool mixed, size_t smem_budget);
 int num_levels_for(int n);
+
+// Programmatic dependent launch for the grid engine's kernels (on by
+// default; DARCY_GPU_PDL=0 turns it off).
+void set_programmatic_launch(bool on);
+bool programmatic_launch();
 
 // ---- launch wrappers (kernels.cu) ----
 void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad, cudaStream_t s);
@@ -99,6 +105,14 @@ void launch_tail_columns(const Lvl64* h_dev, const Lvl64* h_host, int l0, int nl
                          int top_calls, int N, double* Td, float* Tf, cudaStream_t s);
 template <class T>
 void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaStream_t s);
+// Fused level visits (pre_sweeps = post_sweeps = 1): tile-staged red+black
+// sweeps + residual + restriction, and prolongation + black+red sweeps
+// (+ r . z on level 0). xin == null: iterate known to be zero.
+template <class T>
+void launch_visit_pre(const Lvl64& H, const T* b, const double* b64, const T* xin, T* xout, T* bc, cudaStream_t s);
+template <class T>
+void launch_visit_post(const Lvl64& H, const T* b, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
+                       double* partials, cudaStream_t s);
 template <class T>
 void launch_dot_rz(const T* z, const double* r, int64_t m, CgState* st, double* partials, cudaStream_t s);
 void launch_precond_diag(const double* r, const double* id, double* z, int64_t m, CgState* st,
@@ -119,6 +133,8 @@ void launch_copy_back(const T* src, double* dst, int64_t m, cudaStream_t s);
 
 template <class T>
 void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream_t s);
+template <class T>
+int block_solve_occupancy(int threads, size_t smem);
 // Block-engine preconditioner only: z = M r for one problem (apply_preconditioner hook).
 template <class T>
 void launch_block_precondition(const BatchArgs& args, const double* r, double* z, int threads, cudaStream_t s);

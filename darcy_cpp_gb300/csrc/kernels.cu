@@ -10,6 +10,7 @@
 
 #include "cycle.cuh"
 #include "engine.h"
+#include "fused.cuh"
 
 namespace dgpu {
 
@@ -20,6 +21,32 @@ static inline int grid_for(int64_t work, int threads = kThreads) {
     if (g < 1) g = 1;
     if (g > kMaxBlocks) g = kMaxBlocks;
     return (int)g;
+}
+
+// Launches of the grid engine go through launch_k: with programmatic
+// serialization on (set_programmatic_launch), graph edges between them become
+// programmatic so each kernel's launch overlaps its predecessor's tail.
+static bool g_pdl = false;
+void set_programmatic_launch(bool on) { g_pdl = on; }
+bool programmatic_launch() { return g_pdl; }
+
+template <typename... KArgs, typename... Args>
+static void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    if (!g_pdl) {
+        kern<<<grid, block, smem, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
 __device__ __forceinline__ void stop_loop(CgState* st) {
@@ -67,21 +94,24 @@ __device__ __forceinline__ double apply_cell(const Lvl64& L, const double* __res
 // ------------------------------------------------------------- setup kernels
 
 __global__ void k_build_fine(const double* __restrict__ a, Lvl64 L, unsigned long long* bad) {
+    pdl_enter();
     build_fine<GridScope>(a, L, bad);
 }
-__global__ void k_coarsen(Lvl64 F, Lvl64 C) { coarsen<GridScope>(F, C); }
+__global__ void k_coarsen(Lvl64 F, Lvl64 C) {
+    pdl_enter(); coarsen<GridScope>(F, C); }
 __global__ void k_to_fp32(Lvl64 L, float* e, float* nf, float* d, float* id) {
+    pdl_enter();
     to_fp32<GridScope>(L, e, nf, d, id);
 }
 
 void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad, cudaStream_t s) {
-    k_build_fine<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(a, L, bad);
+    launch_k(k_build_fine, grid_for((int64_t)L.n * L.n), kThreads, 0, s, a, L, bad);
 }
 void launch_coarsen(const Lvl64& F, const Lvl64& C, cudaStream_t s) {
-    k_coarsen<<<grid_for((int64_t)C.n * C.n), kThreads, 0, s>>>(F, C);
+    launch_k(k_coarsen, grid_for((int64_t)C.n * C.n), kThreads, 0, s, F, C);
 }
 void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, cudaStream_t s) {
-    k_to_fp32<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, e, nf, d, id);
+    launch_k(k_to_fp32, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, e, nf, d, id);
 }
 
 // ---------------------------------------------------------------- PCG kernels
@@ -92,6 +122,7 @@ __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
                           double* __restrict__ b, double* __restrict__ r, double* __restrict__ u,
                           double* __restrict__ p, float* __restrict__ b0f, const double* __restrict__ u0,
                           Lvl64 L0, CgState* st, double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     double sb = 0.0, sr = 0.0;
     const int n = L0.n;
@@ -100,7 +131,7 @@ __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
         const double bk = (f ? f[k] : fscalar) * h2;
         double rk = bk;
         if (u0) {
-            const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+            const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
             rk = bk - apply_cell(L0, u0, i, j);
             u[k] = u0[k];
         } else {
@@ -143,16 +174,19 @@ __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
 // converged iteration's remaining graph nodes cost only their launch.
 template <class T>
 __global__ void k_gs(Lvl<T> L, int c, bool zero, const CgState* st) {
+    pdl_enter();
     if (st && st->done) return;
     gs_colour<GridScope>(L, c, zero);
 }
 template <class T>
 __global__ void k_residual_restrict(Lvl<T> L, T* bc, const CgState* st) {
+    pdl_enter();
     if (st && st->done) return;
     residual_restrict<GridScope>(L, bc);
 }
 template <class T>
 __global__ void k_prolong_gs1(Lvl<T> L, const T* xc, const CgState* st) {
+    pdl_enter();
     if (st && st->done) return;
     prolong_gs1<GridScope>(L, xc);
 }
@@ -162,6 +196,7 @@ __global__ void k_prolong_gs1(Lvl<T> L, const T* xc, const CgState* st) {
 // mixed form it is the FP32 iterate widened to FP64 on the fly.
 template <class T>
 __global__ void k_gs0_dot(Lvl<T> L, const double* __restrict__ r, CgState* st, double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     if (st->done) return;
     const int n = L.n;
@@ -200,6 +235,7 @@ __global__ void k_gs0_dot(Lvl<T> L, const double* __restrict__ r, CgState* st, d
 template <class T>
 __global__ void k_dot_rz(const T* __restrict__ z, const double* __restrict__ r, int64_t m, CgState* st,
                          double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     if (st->done) return;
     double acc = 0.0;
@@ -216,6 +252,7 @@ __global__ void k_dot_rz(const T* __restrict__ z, const double* __restrict__ r, 
 // (solver.hpp:122-137, :167-171). id == null selects "none".
 __global__ void k_precond_diag(const double* __restrict__ r, const double* __restrict__ id,
                                double* __restrict__ z, int64_t m, CgState* st, double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     if (st->done) return;
     double acc = 0.0;
@@ -236,6 +273,7 @@ __global__ void k_precond_diag(const double* __restrict__ r, const double* __res
 // also where a finished solve stops the device-side while loop.
 template <class Z>
 __global__ void k_xpby(const Z* __restrict__ z, double* __restrict__ p, int64_t m, CgState* st) {
+    pdl_enter();
     if (st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) stop_loop(st);
         return;
@@ -247,13 +285,14 @@ __global__ void k_xpby(const Z* __restrict__ z, double* __restrict__ p, int64_t 
 // ap = A p and p . Ap, then alpha or a breakdown (solver.hpp:147-156).
 __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __restrict__ ap, CgState* st,
                             double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     if (st->done) return;
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
     double acc = 0.0;
     for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
-        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
         const double y = apply_cell(L, p, i, j);
         ap[k] = y;
         acc += p[k] * y;
@@ -280,6 +319,7 @@ __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __res
 __global__ void k_cg_update(const double* __restrict__ p, const double* __restrict__ ap, double* __restrict__ u,
                             double* __restrict__ r, float* __restrict__ b0f, const float* __restrict__ zold,
                             int64_t m, CgState* st, double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     if (st->done) return;
     const double alpha = st->alpha;
@@ -315,6 +355,7 @@ __global__ void k_cg_update(const double* __restrict__ p, const double* __restri
 // when ||b|| == 0 (f == 0 returns u == 0 whatever the warm start).
 __global__ void k_true_residual(Lvl64 L, double* __restrict__ u, const double* __restrict__ b, CgState* st,
                                 double* partials) {
+    pdl_enter();
     __shared__ double red[32];
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
@@ -325,7 +366,7 @@ __global__ void k_true_residual(Lvl64 L, double* __restrict__ u, const double* _
             u[k] = 0.0;
             continue;
         }
-        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
         const double rk = b[k] - apply_cell(L, u, i, j);
         acc += rk * rk;
     }
@@ -335,20 +376,23 @@ __global__ void k_true_residual(Lvl64 L, double* __restrict__ u, const double* _
 }
 
 __global__ void k_apply(Lvl64 L, const double* __restrict__ x, double* __restrict__ y) {
+    pdl_enter();
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
     for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
-        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
         y[k] = apply_cell(L, x, i, j);
     }
 }
 
 template <class T>
 __global__ void k_copy_cast(const double* __restrict__ src, T* __restrict__ dst, int64_t m) {
+    pdl_enter();
     for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) dst[k] = (T)src[k];
 }
 template <class T>
 __global__ void k_copy_back(const T* __restrict__ src, double* __restrict__ dst, int64_t m) {
+    pdl_enter();
     for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) dst[k] = (double)src[k];
 }
 
@@ -356,6 +400,7 @@ __global__ void k_copy_back(const T* __restrict__ src, double* __restrict__ dst,
 template <class T>
 __global__ void k_tail(const Lvl<T>* __restrict__ lv, int l0, int nlev, int pre, int post, int gamma,
                        int top_calls, const double* id64, const CgState* st) {
+    pdl_enter();
     if (st && st->done) return;
     block_cycle<T>(lv, l0, nlev, pre, post, gamma, top_calls, id64);
 }
@@ -368,6 +413,7 @@ __global__ void k_tail(const Lvl<T>* __restrict__ lv, int l0, int nlev, int pre,
 // row-major, FP64 and optionally rounded to FP32 for the mixed form.
 __global__ void k_tail_columns(const Lvl64* __restrict__ h, int l0, int nlev, int pre, int post, int gamma,
                                int top_calls, int N, double* __restrict__ Td, float* __restrict__ Tf) {
+    pdl_enter();
     extern __shared__ double sm_vec[];
     __shared__ Lvl<double> lv[kMaxLevels];
     if (threadIdx.x == 0) {
@@ -399,25 +445,88 @@ __device__ __forceinline__ T warp_sum_t(T v) {
     return v;
 }
 
-// x_{l0} = T b_{l0}: one warp per row, b staged in shared memory.
+// x_{l0} = T b_{l0}: one warp per row, b staged in shared memory, the row
+// streamed with 16-byte loads (N is a square of a side <= 32; rows of
+// N % 4 == 0 are read as 16-byte vectors, others scalar).
 template <class T>
-__global__ void k_tail_matvec(const T* __restrict__ M, int N, const T* __restrict__ b, T* __restrict__ x,
-                              const CgState* st) {
-    if (st && st->done) return;
-    extern __shared__ unsigned char sm_raw[];
-    T* bs = reinterpret_cast<T*>(sm_raw);
-    for (int k = threadIdx.x; k < N; k += blockDim.x) bs[k] = b[k];
-    __syncthreads();
+__device__ __forceinline__ T dot_row(const T* __restrict__ Mr, const T* __restrict__ b, int N, int lane) {
+    T acc = T(0);
+    if ((N & 3) == 0 && sizeof(T) == 4) {
+        const float4* M4 = reinterpret_cast<const float4*>(Mr);
+        const float4* b4 = reinterpret_cast<const float4*>(b);
+#pragma unroll 8
+        for (int c = lane; c < (N >> 2); c += 32) {
+            const float4 m = __ldg(M4 + c), v = __ldg(b4 + c);
+            acc += (T)m.x * (T)v.x + (T)m.y * (T)v.y + (T)m.z * (T)v.z + (T)m.w * (T)v.w;
+        }
+    } else if ((N & 1) == 0 && sizeof(T) == 8) {
+        const double2* M2 = reinterpret_cast<const double2*>(Mr);
+        const double2* b2 = reinterpret_cast<const double2*>(b);
+#pragma unroll 8
+        for (int c = lane; c < (N >> 1); c += 32) {
+            const double2 m = __ldg(M2 + c), v = __ldg(b2 + c);
+            acc += (T)m.x * (T)v.x;
+            acc += (T)m.y * (T)v.y;
+        }
+    } else {
+        for (int c = lane; c < N; c += 32) acc += Mr[c] * b[c];
+    }
+    return warp_sum_t(acc);
+}
+
+// x_{l0} = T b_{l0}: one warp per row; the row streamed with 16-byte loads
+// (rows of N % 4 == 0 floats / N % 2 == 0 doubles; scalar otherwise), b read
+// through the read-only cache by every warp.
+template <class T>
+__global__ void __launch_bounds__(128) k_tail_matvec(const T* __restrict__ M, int N, const T* __restrict__ b,
+                                                     T* __restrict__ x, const CgState* st) {
+    (void)st;  // scratch-only output: runs to completion even after convergence
     const int lane = threadIdx.x & 31;
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    // T is constant during a solve: bring this warp's first row towards the SM
+    // before waiting for the kernel that produces b.
+    if (warp < N) {
+        const char* row = reinterpret_cast<const char*>(M + (size_t)warp * N);
+        for (int off = lane * 128; off < N * (int)sizeof(T); off += 32 * 128)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + off));
+    }
+    pdl_enter();
     for (int row = warp; row < N; row += nwarps) {
-        const T* Mr = M + (size_t)row * N;
-        T acc = T(0);
-        for (int c = lane; c < N; c += 32) acc += Mr[c] * bs[c];
-        acc = warp_sum_t(acc);
+        const T acc = dot_row<T>(M + (size_t)row * N, b, N, lane);
         if (lane == 0) x[row] = acc;
     }
+}
+
+// Fused visit kernels (fused.cuh): 16 x 32 tiles with 256 threads on large
+// levels; 8 x 16 tiles with 128 threads where a level has few cells, so that
+// small levels spread over more SMs and each thread stages less.
+constexpr int kMaxTileGrid = kMaxBlocks;
+
+template <int TH, int TW>
+static inline int tiles_grid(int n) {
+    const int64_t t = (int64_t)((n + TH - 1) / TH) * ((n + TW - 1) / TW);
+    return (int)(t < kMaxTileGrid ? t : kMaxTileGrid);
+}
+
+template <class T>
+void launch_visit_pre(const Lvl64& H, const T* b, const double* b64, const T* xin, T* xout, T* bc, cudaStream_t s) {
+    if (H.n <= 256)
+        launch_k(k_visit_pre<T, 8, 16>, tiles_grid<8, 16>(H.n), 128, VisitSmem<T, 8, 16>::bytes, s, H, b, b64, xin,
+                 xout, bc);
+    else
+        launch_k(k_visit_pre<T, 16, 32>, tiles_grid<16, 32>(H.n), 256, VisitSmem<T, 16, 32>::bytes, s, H, b, b64,
+                 xin, xout, bc);
+}
+template <class T>
+void launch_visit_post(const Lvl64& H, const T* b, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
+                       double* partials, cudaStream_t s) {
+    if (H.n <= 256)
+        launch_k(k_visit_post<T, 8, 16>, tiles_grid<8, 16>(H.n), 128, PostSmem<T, 8, 16>::bytes, s, H, b, xin, xc,
+                 xout, r, st, partials);
+    else
+        launch_k(k_visit_post<T, 16, 32>, tiles_grid<16, 32>(H.n), 256, PostSmem<T, 16, 32>::bytes, s, H, b, xin, xc,
+                 xout, r, st, partials);
 }
 
 // ------------------------------------------------------------ launch wrappers
@@ -425,29 +534,29 @@ __global__ void k_tail_matvec(const T* __restrict__ M, int N, const T* __restric
 void launch_cg_init(const double* f, double h2, int64_t m, double* b, double* r, double* u, double* p,
                     float* b0f, const double* u0, const Lvl64& L0, CgState* st, double* partials,
                     cudaStream_t s) {
-    k_cg_init<<<grid_for(m), kThreads, 0, s>>>(f, h2, m, b, r, u, p, b0f, u0, L0, st, partials);
+    launch_k(k_cg_init, grid_for(m), kThreads, 0, s, f, h2, m, b, r, u, p, b0f, u0, L0, st, partials);
 }
 template <class T>
 void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s) {
-    k_gs<T><<<grid_for(colour_count(L.n, colour)), kThreads, 0, s>>>(L, colour, zero, st);
+    launch_k(k_gs<T>, grid_for(colour_count(L.n, colour)), kThreads, 0, s, L, colour, zero, st);
 }
 template <class T>
 void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s) {
     const int64_t nc = (L.n + 1) / 2;
-    k_residual_restrict<T><<<grid_for(nc * nc), kThreads, 0, s>>>(L, bc, st);
+    launch_k(k_residual_restrict<T>, grid_for(nc * nc), kThreads, 0, s, L, bc, st);
 }
 template <class T>
 void launch_prolong_gs1(const Lvl<T>& L, const T* xc, CgState* st, cudaStream_t s) {
-    k_prolong_gs1<T><<<grid_for(colour_count(L.n, 1)), kThreads, 0, s>>>(L, xc, st);
+    launch_k(k_prolong_gs1<T>, grid_for(colour_count(L.n, 1)), kThreads, 0, s, L, xc, st);
 }
 template <class T>
 void launch_gs0_dot(const Lvl<T>& L, const double* r, CgState* st, double* partials, cudaStream_t s) {
-    k_gs0_dot<T><<<grid_for(colour_count(L.n, 0)), kThreads, 0, s>>>(L, r, st, partials);
+    launch_k(k_gs0_dot<T>, grid_for(colour_count(L.n, 0)), kThreads, 0, s, L, r, st, partials);
 }
 template <class T>
 void launch_tail(const Lvl<T>* lv_dev, int l0, int nlev, int pre, int post, int gamma, int top_calls,
                  const double* id64, CgState* st, int threads, cudaStream_t s) {
-    k_tail<T><<<1, threads, 0, s>>>(lv_dev, l0, nlev, pre, post, gamma, top_calls, id64, st);
+    launch_k(k_tail<T>, 1, threads, 0, s, lv_dev, l0, nlev, pre, post, gamma, top_calls, id64, st);
 }
 void launch_tail_columns(const Lvl64* h_dev, const Lvl64* h_host, int l0, int nlev, int pre, int post, int gamma,
                          int top_calls, int N, double* Td, float* Tf, cudaStream_t s) {
@@ -455,65 +564,79 @@ void launch_tail_columns(const Lvl64* h_dev, const Lvl64* h_host, int l0, int nl
     for (int l = l0; l < nlev; ++l) smem += 2 * sizeof(double) * (size_t)h_host[l].n * h_host[l].n;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_tail_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tail_columns<<<N, 256, smem, s>>>(h_dev, l0, nlev, pre, post, gamma, top_calls, N, Td, Tf);
+    launch_k(k_tail_columns, N, 256, smem, s, h_dev, l0, nlev, pre, post, gamma, top_calls, N, Td, Tf);
 }
 template <class T>
 void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaStream_t s) {
-    const int threads = 256;
+    const int threads = 128;
     int blocks = (N + threads / 32 - 1) / (threads / 32);
     if (blocks > kMaxBlocks) blocks = kMaxBlocks;
-    k_tail_matvec<T><<<blocks, threads, sizeof(T) * (size_t)N, s>>>(M, N, b, x, st);
+    launch_k(k_tail_matvec<T>, blocks, threads, 0, s, M, N, b, x, st);
 }
 template <class T>
 void launch_dot_rz(const T* z, const double* r, int64_t m, CgState* st, double* partials, cudaStream_t s) {
-    k_dot_rz<T><<<grid_for(m), kThreads, 0, s>>>(z, r, m, st, partials);
+    launch_k(k_dot_rz<T>, grid_for(m), kThreads, 0, s, z, r, m, st, partials);
 }
 void launch_precond_diag(const double* r, const double* id, double* z, int64_t m, CgState* st,
                          double* partials, cudaStream_t s) {
-    k_precond_diag<<<grid_for(m), kThreads, 0, s>>>(r, id, z, m, st, partials);
+    launch_k(k_precond_diag, grid_for(m), kThreads, 0, s, r, id, z, m, st, partials);
 }
 template <class Z>
 void launch_xpby(const Z* z, double* p, int64_t m, CgState* st, cudaStream_t s) {
-    k_xpby<Z><<<grid_for(m), kThreads, 0, s>>>(z, p, m, st);
+    launch_k(k_xpby<Z>, grid_for(m), kThreads, 0, s, z, p, m, st);
 }
 void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, double* partials,
                       cudaStream_t s) {
-    k_apply_dot<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, p, ap, st, partials);
+    launch_k(k_apply_dot, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, p, ap, st, partials);
 }
 void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, const float* zold,
                       int64_t m, CgState* st, double* partials, cudaStream_t s) {
-    k_cg_update<<<grid_for(m), kThreads, 0, s>>>(p, ap, u, r, b0f, zold, m, st, partials);
+    launch_k(k_cg_update, grid_for(m), kThreads, 0, s, p, ap, u, r, b0f, zold, m, st, partials);
 }
 void launch_true_residual(const Lvl64& L, const double* u, const double* b, double*, CgState* st,
                           double* partials, cudaStream_t s) {
-    k_true_residual<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, const_cast<double*>(u), b, st,
-                                                                      partials);
+    launch_k(k_true_residual, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, const_cast<double*>(u), b, st, partials);
 }
 void launch_apply(const Lvl64& L, const double* x, double* y, cudaStream_t s) {
-    k_apply<<<grid_for((int64_t)L.n * L.n), kThreads, 0, s>>>(L, x, y);
+    launch_k(k_apply, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, x, y);
 }
 template <class T>
 void launch_copy_cast(const double* src, T* dst, int64_t m, cudaStream_t s) {
-    k_copy_cast<T><<<grid_for(m), kThreads, 0, s>>>(src, dst, m);
+    launch_k(k_copy_cast<T>, grid_for(m), kThreads, 0, s, src, dst, m);
 }
 template <class T>
 void launch_copy_back(const T* src, double* dst, int64_t m, cudaStream_t s) {
-    k_copy_back<T><<<grid_for(m), kThreads, 0, s>>>(src, dst, m);
+    launch_k(k_copy_back<T>, grid_for(m), kThreads, 0, s, src, dst, m);
 }
 
 // ================================================================ block engine
 
-// Per-CTA arena layout for one side-n problem: FP64 hierarchy (e, nf, d, id
-// per level, wb/sb boundary vectors), the FP32 coefficient copies when the
-// cycle runs in FP32, the per-level iterate/right-hand side, and the five
-// FP64 CG vectors b, r, p, Ap, z. Level 0 of an FP64 cycle works directly on
-// r (right-hand side) and z (iterate). Shared by host sizing and device carving.
+// Per-CTA layout for one side-n problem. Global arena (L2-resident while the
+// CTA works on the problem): the FP64 hierarchy (e, nf, d, id per level,
+// wb/sb boundary vectors), the five FP64 CG vectors b, r, p, Ap, z, and the
+// cycle's own coefficient copies and iterate/right-hand side for the large
+// levels. Shared memory: the same for every level from `ls` down, as many
+// coarse levels as fit in `sbudget` bytes -- the W-cycle visits level l 2^l
+// times, so the coarse levels are the ones whose latency matters. Level 0 of
+// an FP64 cycle works directly on r (right-hand side) and z (iterate).
+// Shared by host sizing and device carving (gbase/sbase == null: size only).
+struct BlockLayout {
+    size_t global_bytes, smem_bytes;
+    int nlev, ls;
+};
+
 template <class T>
-__host__ __device__ size_t carve(int n, char* base, Lvl64* h, Lvl<T>* lv, double** cg, int* nlev_out) {
-    size_t off = 0;
-    auto take = [&](size_t bytes) -> char* {
-        char* ptr = base ? base + off : nullptr;
-        off += (bytes + 255) & ~(size_t)255;
+__host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sbudget, Lvl64* h, Lvl<T>* lv,
+                                      double** cg) {
+    size_t goff = 0, soff = 0;
+    auto gtake = [&](size_t bytes) -> char* {
+        char* ptr = gbase ? gbase + goff : nullptr;
+        goff += (bytes + 255) & ~(size_t)255;
+        return ptr;
+    };
+    auto stake = [&](size_t bytes) -> char* {
+        char* ptr = sbase ? sbase + soff : nullptr;
+        soff += (bytes + 15) & ~(size_t)15;
         return ptr;
     };
     int sides[kMaxLevels];
@@ -523,38 +646,48 @@ __host__ __device__ size_t carve(int n, char* base, Lvl64* h, Lvl<T>* lv, double
         if (s <= 1) break;
         s = (s + 1) / 2;
     }
+    int ls = nlev;
+    size_t need = 0;
+    for (int l = nlev - 1; l >= 1; --l) {
+        const size_t lvl = 6 * (((size_t)sides[l] * sides[l] * sizeof(T) + 15) & ~(size_t)15);
+        if (need + lvl > sbudget) break;
+        need += lvl;
+        ls = l;
+    }
     const bool fp32 = sizeof(T) == 4;
     const size_t m0 = (size_t)n * n;
     for (int l = 0; l < nlev; ++l) {
         const size_t m = (size_t)sides[l] * sides[l];
         Lvl64 H;
         H.n = sides[l];
-        H.e = (double*)take(8 * m);
-        H.nf = (double*)take(8 * m);
-        H.d = (double*)take(8 * m);
-        H.id = (double*)take(8 * m);
-        H.wb = (double*)take(8 * (size_t)sides[l]);
-        H.sb = (double*)take(8 * (size_t)sides[l]);
+        H.e = (double*)gtake(8 * m);
+        H.nf = (double*)gtake(8 * m);
+        H.d = (double*)gtake(8 * m);
+        H.id = (double*)gtake(8 * m);
+        H.wb = (double*)gtake(8 * (size_t)sides[l]);
+        H.sb = (double*)gtake(8 * (size_t)sides[l]);
         if (h) h[l] = H;
     }
     double* v[5];
-    for (int q = 0; q < 5; ++q) v[q] = (double*)take(8 * m0);
+    for (int q = 0; q < 5; ++q) v[q] = (double*)gtake(8 * m0);
     if (cg)
         for (int q = 0; q < 5; ++q) cg[q] = v[q];
     for (int l = 0; l < nlev; ++l) {
         const size_t m = (size_t)sides[l] * sides[l];
+        const bool shared = l >= ls;
+        auto take = [&](size_t bytes) { return shared ? stake(bytes) : gtake(bytes); };
         Lvl<T> V;
         V.n = sides[l];
-        if (fp32) {
-            V.e = (const T*)take(4 * m);
-            V.nf = (const T*)take(4 * m);
-            V.d = (const T*)take(4 * m);
-            V.id = (const T*)take(4 * m);
-        } else if (h) {
-            V.e = (const T*)h[l].e;
-            V.nf = (const T*)h[l].nf;
-            V.d = (const T*)h[l].d;
-            V.id = (const T*)h[l].id;
+        if (fp32 || shared) {
+            V.e = (const T*)take(sizeof(T) * m);
+            V.nf = (const T*)take(sizeof(T) * m);
+            V.d = (const T*)take(sizeof(T) * m);
+            V.id = (const T*)take(sizeof(T) * m);
+        } else {
+            V.e = h ? (const T*)h[l].e : nullptr;
+            V.nf = h ? (const T*)h[l].nf : nullptr;
+            V.d = h ? (const T*)h[l].d : nullptr;
+            V.id = h ? (const T*)h[l].id : nullptr;
         }
         if (l == 0 && !fp32) {
             V.x = (T*)v[4];  // z
@@ -565,19 +698,28 @@ __host__ __device__ size_t carve(int n, char* base, Lvl64* h, Lvl<T>* lv, double
         }
         if (lv) lv[l] = V;
     }
-    if (nlev_out) *nlev_out = nlev;
-    return off;
+    return BlockLayout{goff, soff, nlev, ls};
 }
 
-int num_levels_for(int n) {
-    int nl = 0;
-    carve<double>(n, nullptr, nullptr, nullptr, nullptr, &nl);
-    return nl;
+int num_levels_for(int n) { return carve<double>(n, nullptr, nullptr, 0, nullptr, nullptr, nullptr).nlev; }
+
+size_t block_arena_bytes(int n, bool mixed, size_t sbudget) {
+    return mixed ? carve<float>(n, nullptr, nullptr, sbudget, nullptr, nullptr, nullptr).global_bytes
+                 : carve<double>(n, nullptr, nullptr, sbudget, nullptr, nullptr, nullptr).global_bytes;
 }
 
-size_t block_arena_bytes(int n, bool mixed) {
-    return mixed ? carve<float>(n, nullptr, nullptr, nullptr, nullptr, nullptr)
-                 : carve<double>(n, nullptr, nullptr, nullptr, nullptr, nullptr);
+// Cycle coefficients of level l in the cycle's precision (FP32 copies for the
+// mixed form, shared-memory copies for the levels held on chip).
+template <class T>
+__device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& V) {
+    if ((const void*)V.e == (const void*)H.e) return;  // FP64 level used in place
+    const int64_t m = (int64_t)H.n * H.n;
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+        ((T*)V.e)[k] = (T)H.e[k];
+        ((T*)V.nf)[k] = (T)H.nf[k];
+        ((T*)V.d)[k] = (T)H.d[k];
+        ((T*)V.id)[k] = (T)H.id[k];
+    }
 }
 
 // y = A x over a block, FP64, returning sum x . y (or x . x when want_xx).
@@ -586,7 +728,7 @@ __device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* 
     const int64_t m = (int64_t)n * n;
     double acc = 0.0;
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
         const double v = apply_cell(L, x, i, j);
         y[k] = v;
         acc += x[k] * v;
@@ -639,10 +781,8 @@ __device__ unsigned long long block_setup(const BatchArgs& A, const double* a, c
         coarsen<BlockScope>(h[l - 1], h[l]);
         __syncthreads();
     }
-    if (sizeof(T) == 4 && A.pc == kPcMultigrid) {
-        for (int l = 0; l < nlev; ++l)
-            to_fp32<BlockScope>(h[l], (float*)lv[l].e, (float*)lv[l].nf, (float*)lv[l].d, (float*)lv[l].id);
-    }
+    if (A.pc == kPcMultigrid)
+        for (int l = 0; l < nlev; ++l) block_copy_coeffs<T>(h[l], lv[l]);
     __syncthreads();
     return *s_bad;
 }
@@ -675,8 +815,9 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, con
     const double* f = A.f ? (A.f_shared ? A.f : A.f + off) : nullptr;
     const double* u0 = A.u0 ? A.u0 + off : nullptr;
     const bool record = A.record_history && A.history && A.count == 1;
-    // FP32 cycle: flexible (Polak-Ribiere) beta, as in the grid engine.
-    const bool flexible = sizeof(T) == 4 && A.pc == kPcMultigrid;
+    // Standard beta, as in the grid engine (the flexible variant measured
+    // worse for the FP32 cycle).
+    constexpr bool flexible = false;
 
     double sb = 0.0;
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
@@ -704,7 +845,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, con
     if (u0) {
         double sr = 0.0;
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-            const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+            const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
             const double rk = b[k] - apply_cell(h[0], u, i, j);
             r[k] = rk;
             sr += rk * rk;
@@ -759,7 +900,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, con
     double tr = 0.0;
     __syncthreads();
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
         const double rk = b[k] - apply_cell(h[0], u, i, j);
         tr += rk * rk;
     }
@@ -782,12 +923,14 @@ __global__ void __launch_bounds__(1024) k_block_solve(BatchArgs A) {
     __shared__ double red[32];
     __shared__ int s_pid, s_nlev;
     __shared__ unsigned long long s_bad;
+    extern __shared__ __align__(16) unsigned char block_smem[];
     char* arena = A.scratch + (size_t)blockIdx.x * A.scratch_stride;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned w = atomicAdd(A.work, 1u);
             s_pid = w < (unsigned)A.count ? A.order[w] : -1;
-            if (s_pid >= 0) carve<T>(A.side[s_pid], arena, h, lv, cg, &s_nlev);
+            if (s_pid >= 0)
+                s_nlev = carve<T>(A.side[s_pid], arena, (char*)block_smem, A.smem_budget, h, lv, cg).nlev;
         }
         __syncthreads();
         const int pid = s_pid;
@@ -806,7 +949,8 @@ __global__ void __launch_bounds__(1024) k_block_precondition(BatchArgs A, const 
     __shared__ double red[32];
     __shared__ int s_nlev;
     __shared__ unsigned long long s_bad;
-    if (threadIdx.x == 0) carve<T>(A.side[0], A.scratch, h, lv, cg, &s_nlev);
+    extern __shared__ __align__(16) unsigned char block_smem[];
+    if (threadIdx.x == 0) s_nlev = carve<T>(A.side[0], A.scratch, (char*)block_smem, A.smem_budget, h, lv, cg).nlev;
     __syncthreads();
     const unsigned long long bad = block_setup<T>(A, A.a, h, lv, s_nlev, &s_bad);
     if (threadIdx.x == 0) A.bad[0] = bad;
@@ -820,12 +964,25 @@ __global__ void __launch_bounds__(1024) k_block_precondition(BatchArgs A, const 
 }
 
 template <class T>
+int block_solve_occupancy(int threads, size_t smem) {
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_block_solve<T>, threads, smem) != cudaSuccess) n = 1;
+    return n;
+}
+template <class T>
 void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream_t s) {
-    k_block_solve<T><<<ctas, threads, 0, s>>>(args);
+    if (args.smem_budget > 48 * 1024)
+        cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)args.smem_budget);
+    k_block_solve<T><<<ctas, threads, args.smem_budget, s>>>(args);
 }
 template <class T>
 void launch_block_precondition(const BatchArgs& args, const double* r, double* z, int threads, cudaStream_t s) {
-    k_block_precondition<T><<<1, threads, 0, s>>>(args, r, z);
+    if (args.smem_budget > 48 * 1024)
+        cudaFuncSetAttribute(k_block_precondition<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)args.smem_budget);
+    k_block_precondition<T><<<1, threads, args.smem_budget, s>>>(args, r, z);
 }
 
 // ------------------------------------------------------ explicit instantiation
@@ -839,10 +996,14 @@ void launch_block_precondition(const BatchArgs& args, const double* r, double* z
                                  cudaStream_t);                                                            \
     template void launch_dot_rz<T>(const T*, const double*, int64_t, CgState*, double*, cudaStream_t);     \
     template void launch_tail_matvec<T>(const T*, int, const T*, T*, CgState*, cudaStream_t);              \
+    template void launch_visit_pre<T>(const Lvl64&, const T*, const double*, const T*, T*, T*, cudaStream_t); \
+    template void launch_visit_post<T>(const Lvl64&, const T*, const T*, const T*, T*, const double*,        \
+                                       CgState*, double*, cudaStream_t);                                   \
     template void launch_xpby<T>(const T*, double*, int64_t, CgState*, cudaStream_t);                      \
     template void launch_copy_cast<T>(const double*, T*, int64_t, cudaStream_t);                           \
     template void launch_copy_back<T>(const T*, double*, int64_t, cudaStream_t);                           \
     template void launch_block_solve<T>(const BatchArgs&, int, int, cudaStream_t);                          \
+    template int block_solve_occupancy<T>(int, size_t);                                                    \
     template void launch_block_precondition<T>(const BatchArgs&, const double*, double*, int, cudaStream_t);
 
 DGPU_INSTANTIATE(double)

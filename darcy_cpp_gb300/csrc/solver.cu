@@ -7,10 +7,13 @@
 // solve is H2D copies, one graph launch, D2H copies. Small and batched solves
 // go to the block engine (one CTA per problem, one launch per batch).
 #include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <sys/stat.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -159,6 +162,10 @@ struct GridPlan {
     std::vector<Lvl64> h;
     std::vector<Lvl<double>> lvd;
     std::vector<Lvl<float>> lvf;
+    // two iterate buffers per level for the fused visit kernels (ping-pong);
+    // as double* for the FP64 cycle, reinterpreted as float* for the FP32 one
+    std::vector<double*> X0, X1;
+    bool fused = false;
     void* lv_dev = nullptr;
     Lvl64* h_dev = nullptr;
     double* Td = nullptr;           // dense coarse-tail operator, FP64
@@ -180,6 +187,11 @@ struct GridPlan {
         for (cudaGraphExec_t g : {exec, ex_pro, ex_chunk, ex_epi, ex_pc})
             if (g) cudaGraphExecDestroy(g);
     }
+};
+
+struct BlockConfigPOD {
+    int threads;
+    size_t smem;
 };
 
 }  // namespace
@@ -204,6 +216,12 @@ struct dgpu_context {
     // apply_operator / hierarchy buffers
     DVec<char> misc;
     int64_t last_launches = 0;
+    // batched-engine autotuning cache
+    std::string device_name;
+    bool tune_loaded = false;
+    std::map<std::string, BlockConfigPOD> tuned;
+    int last_block_threads = 0;
+    size_t last_block_smem = 0;
 };
 
 namespace {
@@ -228,6 +246,9 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
     P.h.assign(P.nlev, Lvl64{});
     P.lvd.assign(P.nlev, Lvl<double>{});
     P.lvf.assign(P.nlev, Lvl<float>{});
+    P.X0.assign(P.nlev, nullptr);
+    P.X1.assign(P.nlev, nullptr);
+    P.fused = K.pre == 1 && K.post == 1;
     auto layout = [&](Carver& A) {
         P.a = A.take<double>(m);
         P.f = A.take<double>(m);
@@ -264,6 +285,14 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
             D.id = H.id;
             double* xv = A.take<double>(ml);
             double* bv = A.take<double>(ml);
+            double* xa = A.take<double>(ml);
+            if (l == 0) {
+                P.X0[0] = xa;
+                P.X1[0] = P.mixed_mg ? (double*)P.x0f : P.z;
+            } else {
+                P.X0[l] = xv;
+                P.X1[l] = xa;
+            }
             if (l == 0) {
                 D.x = P.z;
                 D.b = P.r;
@@ -346,6 +375,36 @@ void emit_visit(GridPlan& P, int l, bool first, cudaStream_t s) {
     }
 }
 
+// Fused visit (pre_sweeps = post_sweeps = 1): two kernels per level visit,
+// iterates alternating between the level's two buffers. `cur` tracks which
+// buffer holds each level's iterate while the host walks the recursion.
+template <class T>
+void emit_visit_fused(GridPlan& P, int l, bool first, std::vector<int>& cur, cudaStream_t s) {
+    const auto& lv = levels_of<T>(P);
+    const PlanKey& K = P.key;
+    auto X = [&](int lvl, int q) { return (T*)(q == 0 ? P.X0[lvl] : P.X1[lvl]); };
+    const Lvl<T>& A = lv[l];
+    const Lvl64& H = P.h[l];
+    // level 0 of the FP32 cycle restricts the residual of the exact FP64 r
+    const double* b64 = (l == 0 && sizeof(T) == 4) ? P.r : nullptr;
+    if (first) {
+        launch_visit_pre<T>(H, A.b, b64, nullptr, X(l, 0), lv[l + 1].b, s);
+        cur[l] = 0;
+    } else {
+        launch_visit_pre<T>(H, A.b, b64, X(l, cur[l]), X(l, cur[l] ^ 1), lv[l + 1].b, s);
+        cur[l] ^= 1;
+    }
+    if (l + 1 >= P.tail_l0) {
+        launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, X(l + 1, 0), P.st, s);
+        cur[l + 1] = 0;
+    } else {
+        for (int g = 0; g < K.gamma; ++g) emit_visit_fused<T>(P, l + 1, g == 0, cur, s);
+    }
+    launch_visit_post<T>(H, A.b, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1), l == 0 ? P.r : nullptr, P.st,
+                         P.partials, s);
+    cur[l] ^= 1;
+}
+
 void emit_setup(GridPlan& P, cudaStream_t s) {
     launch_build_fine(P.a, P.h[0], &P.st->bad, s);
     for (int l = 1; l < P.nlev; ++l) launch_coarsen(P.h[l - 1], P.h[l], s);
@@ -373,6 +432,13 @@ void emit_precondition(GridPlan& P, cudaStream_t s) {
                 launch_tail_matvec<double>(P.Td, P.ntail, P.r, P.z, P.st, s);
                 launch_dot_rz<double>(P.z, P.r, P.m, P.st, P.partials, s);
             }
+        } else if (P.fused) {
+            // level 0 ends in X1[0] (pre writes X0, post writes X1): z / x0f
+            std::vector<int> cur(P.nlev, 0);
+            if (P.mixed_mg)
+                emit_visit_fused<float>(P, 0, true, cur, s);
+            else
+                emit_visit_fused<double>(P, 0, true, cur, s);
         } else if (P.mixed_mg) {
             emit_visit<float>(P, 0, true, s);
         } else {
@@ -397,8 +463,10 @@ void emit_body(GridPlan& P, cudaStream_t s) {
     else
         launch_xpby<double>(P.z, P.p, P.m, P.st, s);
     launch_apply_dot(P.h[0], P.p, P.ap, P.st, P.partials, s);
-    launch_cg_update(P.p, P.ap, P.u, P.r, P.mixed_mg ? P.b0f : nullptr, P.mixed_mg ? P.x0f : nullptr, P.m, P.st,
-                     P.partials, s);
+    // Standard beta in both forms: the flexible (Polak-Ribiere) beta that
+    // k_cg_update supports measured worse for the FP32 cycle (1024^2 at 1e6
+    // contrast: 127 iterations against 114 with the standard beta).
+    launch_cg_update(P.p, P.ap, P.u, P.r, P.mixed_mg ? P.b0f : nullptr, nullptr, P.m, P.st, P.partials, s);
     emit_precondition(P, s);
 }
 
@@ -601,12 +669,81 @@ struct BatchOut {
     double* history;
 };
 
-int threads_for_side(int side) {
-    const int64_t cells = (int64_t)side * side;
-    int t = 64;
-    while (t < 512 && t * 8 < cells) t *= 2;
-    return t;
+// ---------------------------------------------------------- block autotuner
+//
+// The batched engine's launch shape -- threads per CTA, how many coarse levels
+// live in shared memory, and so how many CTAs share an SM -- is picked per
+// (size bucket, form, preconditioner, cycle) by timing the candidates on a
+// sample of the actual batch (its largest problems), and cached in the
+// context and in a JSON file (DARCY_GPU_TUNE_FILE, default
+// _build/autotune.json beside the library).
+
+struct BlockConfig {
+    int threads = 256;
+    size_t smem = 0;
+};
+
+int size_bucket(int side) {
+    int b = 8;
+    while (b < side) b <<= 1;
+    return b;
 }
+
+std::string tune_file() {
+    if (const char* env = std::getenv("DARCY_GPU_TUNE_FILE")) return env;
+    Dl_info info;
+    if (dladdr((void*)&dgpu_create, &info) && info.dli_fname) {
+        std::string path = info.dli_fname;
+        const size_t slash = path.rfind('/');
+        return (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/_build/autotune.json";
+    }
+    return "autotune.json";
+}
+
+// The cache file is one JSON object: {"<device>|<key>": [threads, smem], ...}.
+void load_tuning(dgpu_context* C) {
+    if (C->tune_loaded) return;
+    C->tune_loaded = true;
+    FILE* fp = std::fopen(tune_file().c_str(), "r");
+    if (!fp) return;
+    std::string text;
+    char buf[4096];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof buf, fp)) > 0) text.append(buf, got);
+    std::fclose(fp);
+    size_t pos = 0;
+    while ((pos = text.find('"', pos)) != std::string::npos) {
+        const size_t end = text.find('"', pos + 1);
+        if (end == std::string::npos) break;
+        const std::string key = text.substr(pos + 1, end - pos - 1);
+        int threads = 0;
+        unsigned long long smem = 0;
+        if (std::sscanf(text.c_str() + end + 1, " : [ %d , %llu ]", &threads, &smem) == 2 && threads > 0)
+            C->tuned[key] = BlockConfigPOD{threads, (size_t)smem};
+        pos = end + 1;
+    }
+}
+
+void save_tuning(dgpu_context* C) {
+    const std::string path = tune_file();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        std::string dir = path.substr(0, slash);
+        std::string cmd_dir = dir;  // create the directory if missing (no shell)
+        mkdir(cmd_dir.c_str(), 0755);
+    }
+    FILE* fp = std::fopen(path.c_str(), "w");
+    if (!fp) return;
+    std::fprintf(fp, "{\n");
+    size_t q = 0;
+    for (const auto& kv : C->tuned)
+        std::fprintf(fp, "  \"%s\": [%d, %zu]%s\n", kv.first.c_str(), kv.second.threads, kv.second.smem,
+                     ++q < C->tuned.size() ? "," : "");
+    std::fprintf(fp, "}\n");
+    std::fclose(fp);
+}
+
+size_t smem_budget_for(bool mixed) { return mixed ? 40 * 1024 : 68 * 1024; }
 
 // Packed problems through the block engine. sides/off on the host; a, f, u0
 // host (or device when device_ptrs) packed arrays.
@@ -623,11 +760,6 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     std::vector<int> order(count);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sides[x] > sides[y]; });
-
-    const int threads = threads_for_side(maxside);
-    const int per_sm = std::max(1, std::min(2048 / threads, 8));
-    const int ctas = (int)std::min<int64_t>(count, (int64_t)C->sms * per_sm);
-    const size_t stride = align_up(block_arena_bytes(maxside, mixed));
 
     BatchArgs A{};
     A.count = (int)count;
@@ -650,8 +782,6 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     A.work = C->bwork.ensure(1);
     A.history = (o->record_history && count == 1) ? C->bhist.ensure((size_t)o->max_iter + 1) : nullptr;
     A.record_history = o->record_history;
-    A.scratch = C->bscratch.ensure(stride * ctas);
-    A.scratch_stride = stride;
     A.tol = o->tol;
     A.max_iter = o->max_iter;
     A.pc = o->preconditioner;
@@ -659,7 +789,6 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     A.post = o->post_sweeps;
     A.gamma = o->cycle_index;
 
-    CK(cudaEventRecord(C->ev0, s));
     CK(cudaMemcpyAsync((void*)A.a, a, sizeof(double) * total, in, s));
     if (f)
         CK(cudaMemcpyAsync((void*)A.f, f, sizeof(double) * (f_shared ? (size_t)sides[0] * sides[0] : (size_t)total),
@@ -668,12 +797,65 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     CK(cudaMemcpyAsync((void*)A.order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)A.side, sides.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)A.off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(A.work, 0, sizeof(unsigned), s));
-    if (mixed)
-        launch_block_solve<float>(A, ctas, threads, s);
-    else
-        launch_block_solve<double>(A, ctas, threads, s);
-    CK(cudaGetLastError());
+
+    // launch with a given shape over the first `n_prob` entries of `order`
+    auto launch = [&](const BlockConfig& cfg, int64_t n_prob) {
+        const int per_sm = mixed ? block_solve_occupancy<float>(cfg.threads, cfg.smem)
+                                 : block_solve_occupancy<double>(cfg.threads, cfg.smem);
+        const int ctas = (int)std::min<int64_t>(n_prob, (int64_t)C->sms * std::max(per_sm, 1));
+        const size_t stride = align_up(block_arena_bytes(maxside, mixed, cfg.smem));
+        BatchArgs B = A;
+        B.count = (int)n_prob;
+        B.scratch = C->bscratch.ensure(stride * ctas);
+        B.scratch_stride = stride;
+        B.smem_budget = cfg.smem;
+        CK(cudaMemsetAsync(B.work, 0, sizeof(unsigned), s));
+        if (mixed)
+            launch_block_solve<float>(B, ctas, cfg.threads, s);
+        else
+            launch_block_solve<double>(B, ctas, cfg.threads, s);
+        CK(cudaGetLastError());
+    };
+
+    char keybuf[160];
+    std::snprintf(keybuf, sizeof keybuf, "%s|side<=%d|%s|pc%d|c%d|s%d%d", C->device_name.c_str(),
+                  size_bucket(maxside), mixed ? "mixed" : "fp64", o->preconditioner, o->cycle_index,
+                  o->pre_sweeps, o->post_sweeps);
+    const std::string key = keybuf;
+    load_tuning(C);
+    BlockConfig cfg;
+    cfg.smem = smem_budget_for(mixed);
+    auto hit = C->tuned.find(key);
+    if (hit != C->tuned.end()) {
+        cfg.threads = hit->second.threads;
+        cfg.smem = hit->second.smem;
+    } else if (count >= C->sms) {
+        // time every candidate on the batch's largest problems
+        const int64_t sample = std::min<int64_t>(count, 2 * (int64_t)C->sms);
+        float best = 1e30f;
+        for (int threads : {128, 256, 512})
+            for (size_t smem : {(size_t)0, smem_budget_for(mixed)}) {
+                const BlockConfig c{threads, smem};
+                launch(c, sample);  // warm (allocations, clocks)
+                CK(cudaEventRecord(C->ev0, s));
+                launch(c, sample);
+                CK(cudaEventRecord(C->ev1, s));
+                CK(cudaEventSynchronize(C->ev1));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, C->ev0, C->ev1));
+                if (ms < best) {
+                    best = ms;
+                    cfg = c;
+                }
+            }
+        C->tuned[key] = BlockConfigPOD{cfg.threads, cfg.smem};
+        save_tuning(C);
+    }
+    C->last_block_threads = cfg.threads;
+    C->last_block_smem = cfg.smem;
+
+    CK(cudaEventRecord(C->ev0, s));
+    launch(cfg, count);
     CK(cudaMemcpyAsync(u_out, A.u, sizeof(double) * total, outk, s));
     std::vector<unsigned long long> bad(count);
     CK(cudaMemcpyAsync(bad.data(), A.bad, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
@@ -843,12 +1025,19 @@ int dgpu_create(int device, dgpu_context** out) {
         cudaDeviceProp prop;
         CK(cudaGetDeviceProperties(&prop, device));
         C->sms = prop.multiProcessorCount;
-        C->cond_ok = conditional_nodes_work(C->stream);
+        C->device_name = prop.name;
+        // DARCY_GPU_LOOP=host selects the host-chunked CG loop (graphs
+        // without conditional nodes, e.g. for per-kernel profiling).
+        const char* loop = std::getenv("DARCY_GPU_LOOP");
+        C->cond_ok = !(loop && std::strcmp(loop, "host") == 0) && conditional_nodes_work(C->stream);
+        const char* pdl = std::getenv("DARCY_GPU_PDL");
+        set_programmatic_launch(!(pdl && std::strcmp(pdl, "0") == 0));
         char buf[512];
-        std::snprintf(buf, sizeof buf, "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s",
+        std::snprintf(buf, sizeof buf,
+                      "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s | programmatic launch: %s",
                       prop.name, prop.multiProcessorCount, prop.major, prop.minor,
                       prop.totalGlobalMem / 1073741824.0, prop.l2CacheSize / 1048576.0,
-                      C->cond_ok ? "device-side" : "host-chunked");
+                      C->cond_ok ? "device-side" : "host-chunked", programmatic_launch() ? "on" : "off");
         C->info = buf;
         *out = C.release();
     });
@@ -937,6 +1126,7 @@ int dgpu_apply_operator(dgpu_context* ctx, const double* a, const double* x, int
     return run([&] {
         if (!ctx) invalid("context must not be NULL");
         if (n < 1) invalid("a must be a square 2-D array with at least one cell");
+        if (n > 46340) invalid("grid size too large for 32-bit cell rows");
         if (!a || !x || !y) invalid("buffers must not be NULL");
         std::lock_guard<std::mutex> lock(ctx->mu);
         CK(cudaSetDevice(ctx->device));
@@ -992,7 +1182,7 @@ int64_t dgpu_hierarchy(dgpu_context* ctx, const double* a, int64_t n, double* ou
     int64_t written = -1;
     int rc = run([&] {
         if (!ctx) invalid("context must not be NULL");
-        if (n < 1 || !a || !out) invalid("bad arguments");
+        if (n < 1 || n > 46340 || !a || !out) invalid("bad arguments");
         std::lock_guard<std::mutex> lock(ctx->mu);
         CK(cudaSetDevice(ctx->device));
         cudaStream_t s = ctx->stream;
@@ -1111,6 +1301,18 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
             const Lvl<T> L1 = levels_of<T>(P)[1];
             const T* Tm = tail_matrix<T>(P);
             // algorithmic bytes: every array the kernel must touch, once
+            if (P.fused) {
+                const Lvl64 H0 = P.h[0];
+                T* xa = (T*)P.X0[0];
+                T* xb = (T*)P.X1[0];
+                T* x1 = (T*)P.X0[1];
+                const double* b64 = sizeof(T) == 4 ? rvec : nullptr;
+                items.push_back({"visit_pre(l0)", 32 * m + w * (2 * m + mc) + (b64 ? 8 * m : 0), 1.0,
+                                 [=] { launch_visit_pre<T>(H0, L0.b, b64, nullptr, xa, L1.b, s); }});
+                items.push_back({"visit_post(l0)", 24 * m + w * (3 * m + mc) + 8 * m, 1.0, [=] {
+                                     launch_visit_post<T>(H0, L0.b, xa, x1, xb, rvec, stp, partials, s);
+                                 }});
+            }
             items.push_back({"gs_colour0_zero(l0)", w * m * 1.5, 1.0, [=] { launch_gs<T>(L0, 0, true, stp, s); }});
             items.push_back({"gs_colour1(l0)", w * (m * 0.5 * 3 + m * 2 + m), 1.0,
                              [=] { launch_gs<T>(L0, 1, false, stp, s); }});
