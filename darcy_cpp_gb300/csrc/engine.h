@@ -66,6 +66,12 @@ struct BatchArgs {
     int record_history;
 };
 
+}  // namespace dgpu
+
+#include "fused.cuh"  // needs CgState
+
+namespace dgpu {
+
 constexpr int kPcNone = 0, kPcJacobi = 1, kPcMultigrid = 2;
 constexpr int kThreads = 256;     // grid-engine block size
 constexpr int kMaxBlocks = 152 * 8;
@@ -84,10 +90,11 @@ bool programmatic_launch();
 // ---- launch wrappers (kernels.cu) ----
 void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad, cudaStream_t s);
 void launch_coarsen(const Lvl64& F, const Lvl64& C, cudaStream_t s);
-void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, cudaStream_t s);
+void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, float* elo, float* nlo, float* dlo,
+                    cudaStream_t s);
 
 void launch_cg_init(const double* f, double h2, int64_t m, double* b, double* r, double* u, double* p,
-                    float* b0f, const double* u0, const Lvl64& L0, CgState* st, double* partials,
+                    float* b0f, float* b0lo, const double* u0, const Lvl64& L0, CgState* st, double* partials,
                     cudaStream_t s);
 template <class T>
 void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s);
@@ -109,9 +116,9 @@ void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaSt
 // sweeps + residual + restriction, and prolongation + black+red sweeps
 // (+ r . z on level 0). xin == null: iterate known to be zero.
 template <class T>
-void launch_visit_pre(const Lvl64& H, const T* b, const double* b64, const T* xin, T* xout, T* bc, cudaStream_t s);
+void launch_visit_pre(const VisitLevel<T>& V, const T* xin, T* xout, T* bc, cudaStream_t s);
 template <class T>
-void launch_visit_post(const Lvl64& H, const T* b, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
+void launch_visit_post(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
                        double* partials, cudaStream_t s);
 template <class T>
 void launch_dot_rz(const T* z, const double* r, int64_t m, CgState* st, double* partials, cudaStream_t s);
@@ -121,8 +128,8 @@ template <class Z>
 void launch_xpby(const Z* z, double* p, int64_t m, CgState* st, cudaStream_t s);
 void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, double* partials,
                       cudaStream_t s);
-void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, const float* zold,
-                      int64_t m, CgState* st, double* partials, cudaStream_t s);
+void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, float* b0lo,
+                      const float* zold, int64_t m, CgState* st, double* partials, cudaStream_t s);
 void launch_true_residual(const Lvl64& L, const double* u, const double* b, double* scratch, CgState* st,
                           double* partials, cudaStream_t s);
 void launch_apply(const Lvl64& L, const double* x, double* y, cudaStream_t s);

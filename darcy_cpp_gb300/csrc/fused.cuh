@@ -13,12 +13,17 @@
 // (x = 0 and face = 0), which reproduces the reference's skipped boundary
 // terms exactly: adding e * 0 leaves the running sum bit-identical.
 //
-// Coefficients are the FP64 hierarchy in both forms. They do not change
-// during a solve, so they are staged before the programmatic-launch wait and
-// their load overlaps the previous kernel. The FP32 form converts them on the
-// fly for its smoothing and keeps the residual it restricts in FP64: at high
-// permeability contrast b - A x cancels to far below the size of its terms,
-// and an FP32 residual there weakens the cycle enough to cost CG iterations.
+// Coefficients do not change during a solve, so they are staged before the
+// programmatic-launch wait and their load overlaps the previous kernel.
+//
+// FP32 cycle (mixed form). Smoothing and transfers run in FP32. The residual
+// that is restricted is formed in double-float arithmetic -- FP32 hi/lo
+// coefficient pairs, error-free products (FMA) and compensated sums -- which
+// is accurate to ~2^-48 of its largest term while using only the FP32 pipes:
+// at high permeability contrast b - A x cancels far below the size of its
+// terms, where a plain FP32 residual weakens the cycle and costs CG
+// iterations, and GB300's FP64 (and FP64<->FP32 conversion) rate is ~1/60 of
+// its FP32 rate.
 //
 // Both kernels read x from one buffer and write another (the halo of a
 // neighbouring tile must see the values from before this pass), so the host
@@ -37,140 +42,213 @@ struct Tile {
     static constexpr int SH = TH + 2 * R, SW = TW + 2 * R, S = SH * SW;
 };
 
-// Stage e, nf, id (and d when ds != null) of the tile + halo.
-template <int TH, int TW, int R>
-__device__ __forceinline__ void stage_coeffs(const Lvl64& H, int ti0, int tj0, double* es, double* ns, double* ds,
-                                             double* is) {
+// Level data a fused visit reads. For T = double: the FP64 hierarchy, lo
+// pointers null. For T = float: FP32 hi parts and the lo parts of e, nf, d
+// (c = hi + lo to ~2^-48); blo is the lo part of b where it exists (level 0).
+template <class T>
+struct VisitLevel {
+    int n;
+    const T* e;
+    const T* nf;
+    const T* d;
+    const T* id;
+    const T* elo;
+    const T* nlo;
+    const T* dlo;
+    const T* b;
+    const T* blo;
+};
+
+// ---------------------------------------------------------- double-float
+struct DF {
+    float hi, lo;
+};
+// s + v, v = (vh, vl) with |vl| << |vh|: TwoSum on the hi parts.
+__device__ __forceinline__ void df_add(DF& s, float vh, float vl) {
+    const float t = s.hi + vh;
+    const float bb = t - s.hi;
+    const float err = (s.hi - (t - bb)) + (vh - bb);
+    s.hi = t;
+    s.lo += err + vl;
+}
+// s += sign * (ch + cl) * x, x exact in FP32: error-free hi product.
+__device__ __forceinline__ void df_axpy(DF& s, float ch, float cl, float x, float sign) {
+    const float p = ch * x;
+    const float pe = fmaf(ch, x, -p);
+    df_add(s, sign * p, sign * (pe + cl * x));
+}
+
+// -------------------------------------------------------------- staging
+
+template <class T, int TH, int TW, int R, bool WITH_D, bool WITH_LO>
+__device__ __forceinline__ void stage_coeffs(const VisitLevel<T>& V, int ti0, int tj0, T* es, T* ns, T* ds, T* is,
+                                             T* elo, T* nlo, T* dlo) {
     using G = Tile<TH, TW, R>;
-    const int n = H.n;
+    const int n = V.n;
     for (int q = threadIdx.x; q < G::S; q += blockDim.x) {
         const int li = q / G::SW, lj = q - li * G::SW;
         const int gi = ti0 - R + li, gj = tj0 - R + lj;
-        double ev = 0.0, nv = 0.0, dv = 0.0, iv = 0.0;
+        T ev = T(0), nv = T(0), dv = T(0), iv = T(0), el = T(0), nl = T(0), dl = T(0);
         if (gi >= 0 && gi < n && gj >= 0 && gj < n) {
             const int k = gi * n + gj;
-            ev = __ldg(H.e + k);
-            nv = __ldg(H.nf + k);
-            if (ds) dv = __ldg(H.d + k);
-            iv = __ldg(H.id + k);
+            ev = __ldg(V.e + k);
+            nv = __ldg(V.nf + k);
+            if (WITH_D) dv = __ldg(V.d + k);
+            iv = __ldg(V.id + k);
+            if (WITH_LO) {
+                el = __ldg(V.elo + k);
+                nl = __ldg(V.nlo + k);
+                if (WITH_D) dl = __ldg(V.dlo + k);
+            }
         }
         es[q] = ev;
         ns[q] = nv;
-        if (ds) ds[q] = dv;
+        if (WITH_D) ds[q] = dv;
         is[q] = iv;
+        if (WITH_LO) {
+            elo[q] = el;
+            nlo[q] = nl;
+            if (WITH_D) dlo[q] = dl;
+        }
     }
 }
 
-// Stage x (+ the prolongation xc[aggregate] when xc != null) and b.
+// x (+ the prolongation xc[aggregate] when xc != null), b and b's lo part.
 template <class T, int TH, int TW, int R>
-__device__ __forceinline__ void stage_vectors(int n, const T* __restrict__ xin, const T* __restrict__ xc,
-                                              const T* __restrict__ b, int ti0, int tj0, T* xs, T* bs) {
+__device__ __forceinline__ void stage_vectors(const VisitLevel<T>& V, const T* __restrict__ xin,
+                                              const T* __restrict__ xc, int ti0, int tj0, T* xs, T* bs, T* bls) {
     using G = Tile<TH, TW, R>;
-    const int nc = (n + 1) >> 1;
+    const int n = V.n, nc = (n + 1) >> 1;
     for (int q = threadIdx.x; q < G::S; q += blockDim.x) {
         const int li = q / G::SW, lj = q - li * G::SW;
         const int gi = ti0 - R + li, gj = tj0 - R + lj;
-        T xv = T(0), bv = T(0);
+        T xv = T(0), bv = T(0), bl = T(0);
         if (gi >= 0 && gi < n && gj >= 0 && gj < n) {
             const int k = gi * n + gj;
             if (xin) xv = xin[k];
             if (xc) xv += xc[(gi >> 1) * nc + (gj >> 1)];
-            bv = b[k];
+            bv = V.b[k];
+            if (bls && V.blo) bl = V.blo[k];
         }
         xs[q] = xv;
         bs[q] = bv;
+        if (bls) bls[q] = bl;
     }
 }
 
-// One colour pass on the staged tile over local rows/cols [lo, SH-lo) x
-// [lo, SW-lo), in-domain cells of colour c only (level.hpp:145-161), in the
-// cycle's precision T.
-template <class T, int TH, int TW, int R>
-__device__ __forceinline__ void stage_gs(int n, int ti0, int tj0, int lo, int c, T* xs, const double* es,
-                                         const double* ns, const double* is, const T* bs) {
+// One colour pass over the in-domain cells of colour c inside local rows /
+// cols [LO, S-LO): every row of the region holds exactly half its cells of
+// each colour (the staged width is even), so cells are enumerated directly.
+template <class T, int TH, int TW, int R, int LO>
+__device__ __forceinline__ void stage_gs(int n, int ti0, int tj0, int c, T* xs, const T* es, const T* ns,
+                                         const T* is, const T* bs) {
     using G = Tile<TH, TW, R>;
-    const int h = G::SH - 2 * lo, w = G::SW - 2 * lo;
-    for (int q = threadIdx.x; q < h * w; q += blockDim.x) {
-        const int li = lo + q / w, lj = lo + (q - (q / w) * w);
-        const int gi = ti0 - R + li, gj = tj0 - R + lj;
-        if (((gi + gj) & 1) != c || gi < 0 || gi >= n || gj < 0 || gj >= n) continue;
+    constexpr int h = G::SH - 2 * LO, hw = (G::SW - 2 * LO) / 2;
+    static_assert((G::SW - 2 * LO) % 2 == 0, "even staged width");
+    for (int q = threadIdx.x; q < h * hw; q += blockDim.x) {
+        const int r = q / hw, k = q - r * hw;
+        const int li = LO + r;
+        const int gi = ti0 - R + li;
+        // first local column of colour c in this row
+        const int par = (c - gi - (tj0 - R) - LO) & 1;
+        const int lj = LO + par + 2 * k;
+        const int gj = tj0 - R + lj;
+        if (gi < 0 || gi >= n || gj < 0 || gj >= n) continue;
         const int s = li * G::SW + lj;
         T v = bs[s];
-        v += (T)es[s] * xs[s + 1];
-        v += (T)es[s - 1] * xs[s - 1];
-        v += (T)ns[s] * xs[s + G::SW];
-        v += (T)ns[s - G::SW] * xs[s - G::SW];
-        xs[s] = v * (T)is[s];
+        v += es[s] * xs[s + 1];
+        v += es[s - 1] * xs[s - 1];
+        v += ns[s] * xs[s + G::SW];
+        v += ns[s - G::SW] * xs[s - G::SW];
+        xs[s] = v * is[s];
     }
 }
 
 template <class T, int TH, int TW>
 struct VisitSmem {
-    static constexpr int R = 3;
-    static constexpr size_t bytes = (sizeof(double) * 4 + sizeof(T) * 2) * Tile<TH, TW, R>::S;
+    // FP64: e, nf, d, id, x, b. FP32: + e_lo, nf_lo, d_lo, b_lo.
+    static constexpr int arrays = sizeof(T) == 8 ? 6 : 10;
+    static constexpr size_t bytes = sizeof(T) * arrays * Tile<TH, TW, 3>::S;
 };
 template <class T, int TH, int TW>
 struct PostSmem {
-    static constexpr size_t bytes = (sizeof(double) * 3 + sizeof(T) * 2) * Tile<TH, TW, 2>::S;
+    static constexpr size_t bytes = sizeof(T) * 5 * Tile<TH, TW, 2>::S;
 };
 
 // Pre-smoothing (1 sweep: red then black), residual, restriction. xin == null
-// means the iterate is known to be zero (first call from the parent). b64,
-// when given, is the level's right-hand side in FP64 (level 0: the CG
-// residual) for the residual; otherwise the staged b is used.
+// means the iterate is known to be zero (first call from the parent).
 template <class T, int TH, int TW>
-__global__ void __launch_bounds__(256) k_visit_pre(Lvl64 H, const T* __restrict__ b, const double* __restrict__ b64,
-                                                   const T* __restrict__ xin, T* __restrict__ xout,
+__global__ void __launch_bounds__(256) k_visit_pre(VisitLevel<T> V, const T* __restrict__ xin, T* __restrict__ xout,
                                                    T* __restrict__ bc) {
     constexpr int R = 3;
+    constexpr bool LO = sizeof(T) == 4;
     using G = Tile<TH, TW, R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double* es = reinterpret_cast<double*>(smem_raw);
-    double* ns = es + G::S;
-    double* ds = ns + G::S;
-    double* is = ds + G::S;
-    T* xs = reinterpret_cast<T*>(is + G::S);
+    T* es = reinterpret_cast<T*>(smem_raw);
+    T* ns = es + G::S;
+    T* ds = ns + G::S;
+    T* is = ds + G::S;
+    T* xs = is + G::S;
     T* bs = xs + G::S;
-    const int n = H.n, nc = (n + 1) >> 1;
+    T* elo = LO ? bs + G::S : nullptr;
+    T* nlo = LO ? elo + G::S : nullptr;
+    T* dlo = LO ? nlo + G::S : nullptr;
+    T* bls = LO ? dlo + G::S : nullptr;
+    const int n = V.n, nc = (n + 1) >> 1;
     const int tiles_x = (n + TW - 1) / TW, tiles = tiles_x * ((n + TH - 1) / TH);
     bool waited = false;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int ti0 = (tile / tiles_x) * TH, tj0 = (tile % tiles_x) * TW;
-        stage_coeffs<TH, TW, R>(H, ti0, tj0, es, ns, ds, is);
+        stage_coeffs<T, TH, TW, R, true, LO>(V, ti0, tj0, es, ns, ds, is, elo, nlo, dlo);
         if (!waited) {  // coefficients are constant: fetched while the predecessor finishes
             pdl_enter();
             waited = true;
         }
-        stage_vectors<T, TH, TW, R>(n, xin, nullptr, b, ti0, tj0, xs, bs);
+        stage_vectors<T, TH, TW, R>(V, xin, nullptr, ti0, tj0, xs, bs, bls);
         __syncthreads();
-        stage_gs<T, TH, TW, R>(n, ti0, tj0, 1, 0, xs, es, ns, is, bs);  // red, rings <= 2
+        stage_gs<T, TH, TW, R, 1>(n, ti0, tj0, 0, xs, es, ns, is, bs);  // red, rings <= 2
         __syncthreads();
-        stage_gs<T, TH, TW, R>(n, ti0, tj0, 2, 1, xs, es, ns, is, bs);  // black, rings <= 1
+        stage_gs<T, TH, TW, R, 2>(n, ti0, tj0, 1, xs, es, ns, is, bs);  // black, rings <= 1
         __syncthreads();
-        // residual of each tile cell in FP64, summed per aggregate
-        // (level.hpp:122-137, :214-227)
+        // residual of each tile cell, summed per aggregate (level.hpp:122-137, :214-227)
         for (int q = threadIdx.x; q < (TH / 2) * (TW / 2); q += blockDim.x) {
             const int ai = q / (TW / 2), aj = q - ai * (TW / 2);
             const int I = (ti0 >> 1) + ai, J = (tj0 >> 1) + aj;
             if (I >= nc || J >= nc) continue;
-            double acc = 0.0;
-            for (int di = 0; di < 2; ++di) {
-                const int gi = 2 * I + di;
-                if (gi >= n) break;
-                for (int dj = 0; dj < 2; ++dj) {
-                    const int gj = 2 * J + dj;
-                    if (gj >= n) break;
-                    const int s = (R + 2 * ai + di) * G::SW + (R + 2 * aj + dj);
-                    double v = ds[s] * (double)xs[s];
-                    v -= es[s] * (double)xs[s + 1];
-                    v -= es[s - 1] * (double)xs[s - 1];
-                    v -= ns[s] * (double)xs[s + G::SW];
-                    v -= ns[s - G::SW] * (double)xs[s - G::SW];
-                    const double bv = b64 ? b64[gi * n + gj] : (double)bs[s];
-                    acc += bv - v;
+            if constexpr (sizeof(T) == 8) {
+                T acc = T(0);
+                for (int di = 0; di < 2; ++di) {
+                    if (2 * I + di >= n) break;
+                    for (int dj = 0; dj < 2; ++dj) {
+                        if (2 * J + dj >= n) break;
+                        const int s = (R + 2 * ai + di) * G::SW + (R + 2 * aj + dj);
+                        T v = ds[s] * xs[s];
+                        v -= es[s] * xs[s + 1];
+                        v -= es[s - 1] * xs[s - 1];
+                        v -= ns[s] * xs[s + G::SW];
+                        v -= ns[s - G::SW] * xs[s - G::SW];
+                        acc += bs[s] - v;
+                    }
                 }
+                bc[I * nc + J] = acc;
+            } else {
+                DF acc{0.f, 0.f};
+                for (int di = 0; di < 2; ++di) {
+                    if (2 * I + di >= n) break;
+                    for (int dj = 0; dj < 2; ++dj) {
+                        if (2 * J + dj >= n) break;
+                        const int s = (R + 2 * ai + di) * G::SW + (R + 2 * aj + dj);
+                        // r = b - d x + e xE + w xW + n xN + s xS
+                        df_add(acc, bs[s], bls[s]);
+                        df_axpy(acc, ds[s], dlo[s], xs[s], -1.f);
+                        df_axpy(acc, es[s], elo[s], xs[s + 1], 1.f);
+                        df_axpy(acc, es[s - 1], elo[s - 1], xs[s - 1], 1.f);
+                        df_axpy(acc, ns[s], nlo[s], xs[s + G::SW], 1.f);
+                        df_axpy(acc, ns[s - G::SW], nlo[s - G::SW], xs[s - G::SW], 1.f);
+                    }
+                }
+                bc[I * nc + J] = acc.hi + acc.lo;
             }
-            bc[I * nc + J] = (T)acc;
         }
         // the smoothed iterate of the tile
         for (int q = threadIdx.x; q < TH * TW; q += blockDim.x) {
@@ -186,34 +264,34 @@ __global__ void __launch_bounds__(256) k_visit_pre(Lvl64 H, const T* __restrict_
 // Prolongation + post-smoothing (1 sweep: black then red). On level 0 (r
 // given) also r . z and beta, like k_gs0_dot.
 template <class T, int TH, int TW>
-__global__ void __launch_bounds__(256) k_visit_post(Lvl64 H, const T* __restrict__ b, const T* __restrict__ xin,
+__global__ void __launch_bounds__(256) k_visit_post(VisitLevel<T> V, const T* __restrict__ xin,
                                                     const T* __restrict__ xc, T* __restrict__ xout,
                                                     const double* __restrict__ r, CgState* st, double* partials) {
     constexpr int R = 2;
     using G = Tile<TH, TW, R>;
     __shared__ double red[32];
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double* es = reinterpret_cast<double*>(smem_raw);
-    double* ns = es + G::S;
-    double* is = ns + G::S;
-    T* xs = reinterpret_cast<T*>(is + G::S);
+    T* es = reinterpret_cast<T*>(smem_raw);
+    T* ns = es + G::S;
+    T* is = ns + G::S;
+    T* xs = is + G::S;
     T* bs = xs + G::S;
-    const int n = H.n;
+    const int n = V.n;
     const int tiles_x = (n + TW - 1) / TW, tiles = tiles_x * ((n + TH - 1) / TH);
     double acc = 0.0;
     bool waited = false;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int ti0 = (tile / tiles_x) * TH, tj0 = (tile % tiles_x) * TW;
-        stage_coeffs<TH, TW, R>(H, ti0, tj0, es, ns, nullptr, is);
+        stage_coeffs<T, TH, TW, R, false, false>(V, ti0, tj0, es, ns, nullptr, is, nullptr, nullptr, nullptr);
         if (!waited) {
             pdl_enter();
             waited = true;
         }
-        stage_vectors<T, TH, TW, R>(n, xin, xc, b, ti0, tj0, xs, bs);
+        stage_vectors<T, TH, TW, R>(V, xin, xc, ti0, tj0, xs, bs, nullptr);
         __syncthreads();
-        stage_gs<T, TH, TW, R>(n, ti0, tj0, 1, 1, xs, es, ns, is, bs);  // black, rings <= 1
+        stage_gs<T, TH, TW, R, 1>(n, ti0, tj0, 1, xs, es, ns, is, bs);  // black, rings <= 1
         __syncthreads();
-        stage_gs<T, TH, TW, R>(n, ti0, tj0, 2, 0, xs, es, ns, is, bs);  // red, ring 0
+        stage_gs<T, TH, TW, R, 2>(n, ti0, tj0, 0, xs, es, ns, is, bs);  // red, ring 0
         __syncthreads();
         for (int q = threadIdx.x; q < TH * TW; q += blockDim.x) {
             const int li = q / TW, lj = q - li * TW;

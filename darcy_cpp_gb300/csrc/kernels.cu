@@ -8,6 +8,7 @@
 //     problem, pulling problems from a work counter, largest first.
 #include <math.h>
 
+#include "block.cuh"
 #include "cycle.cuh"
 #include "engine.h"
 #include "fused.cuh"
@@ -79,17 +80,6 @@ __device__ __forceinline__ bool grid_sum2_last(double v1, double v2, double* par
     return true;
 }
 
-// y = A x at one cell, FP64 (level.hpp:105-119).
-__device__ __forceinline__ double apply_cell(const Lvl64& L, const double* __restrict__ x, int i, int j) {
-    const int n = L.n;
-    const int64_t k = (int64_t)i * n + j;
-    double v = L.d[k] * x[k];
-    if (j + 1 < n) v -= L.e[k] * x[k + 1];
-    if (j > 0) v -= L.e[k - 1] * x[k - 1];
-    if (i + 1 < n) v -= L.nf[k] * x[k + n];
-    if (i > 0) v -= L.nf[k - n] * x[k - n];
-    return v;
-}
 
 // ------------------------------------------------------------- setup kernels
 
@@ -99,9 +89,9 @@ __global__ void k_build_fine(const double* __restrict__ a, Lvl64 L, unsigned lon
 }
 __global__ void k_coarsen(Lvl64 F, Lvl64 C) {
     pdl_enter(); coarsen<GridScope>(F, C); }
-__global__ void k_to_fp32(Lvl64 L, float* e, float* nf, float* d, float* id) {
+__global__ void k_to_fp32(Lvl64 L, float* e, float* nf, float* d, float* id, float* elo, float* nlo, float* dlo) {
     pdl_enter();
-    to_fp32<GridScope>(L, e, nf, d, id);
+    to_fp32<GridScope>(L, e, nf, d, id, elo, nlo, dlo);
 }
 
 void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad, cudaStream_t s) {
@@ -110,8 +100,9 @@ void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad,
 void launch_coarsen(const Lvl64& F, const Lvl64& C, cudaStream_t s) {
     launch_k(k_coarsen, grid_for((int64_t)C.n * C.n), kThreads, 0, s, F, C);
 }
-void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, cudaStream_t s) {
-    launch_k(k_to_fp32, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, e, nf, d, id);
+void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, float* elo, float* nlo, float* dlo,
+                    cudaStream_t s) {
+    launch_k(k_to_fp32, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, e, nf, d, id, elo, nlo, dlo);
 }
 
 // ---------------------------------------------------------------- PCG kernels
@@ -120,8 +111,8 @@ void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, cu
 // (or u0), p = 0, ||b|| and the initial residual (solver.hpp:104-108, :143-144).
 __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
                           double* __restrict__ b, double* __restrict__ r, double* __restrict__ u,
-                          double* __restrict__ p, float* __restrict__ b0f, const double* __restrict__ u0,
-                          Lvl64 L0, CgState* st, double* partials) {
+                          double* __restrict__ p, float* __restrict__ b0f, float* __restrict__ b0lo,
+                          const double* __restrict__ u0, Lvl64 L0, CgState* st, double* partials) {
     pdl_enter();
     __shared__ double red[32];
     double sb = 0.0, sr = 0.0;
@@ -140,7 +131,11 @@ __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
         b[k] = bk;
         r[k] = rk;
         p[k] = 0.0;
-        if (b0f) b0f[k] = (float)rk;
+        if (b0f) {
+            const float hi = (float)rk;
+            b0f[k] = hi;
+            b0lo[k] = (float)(rk - (double)hi);
+        }
         sb += bk * bk;
         sr += rk * rk;
     }
@@ -317,8 +312,8 @@ __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __res
 // and beta = r_new.(z_new - z_old) / r_old.z_old keeps CG's convergence rate
 // with it. For an exact preconditioner r_new . z_old = 0 and the two betas agree.
 __global__ void k_cg_update(const double* __restrict__ p, const double* __restrict__ ap, double* __restrict__ u,
-                            double* __restrict__ r, float* __restrict__ b0f, const float* __restrict__ zold,
-                            int64_t m, CgState* st, double* partials) {
+                            double* __restrict__ r, float* __restrict__ b0f, float* __restrict__ b0lo,
+                            const float* __restrict__ zold, int64_t m, CgState* st, double* partials) {
     pdl_enter();
     __shared__ double red[32];
     if (st->done) return;
@@ -328,7 +323,11 @@ __global__ void k_cg_update(const double* __restrict__ p, const double* __restri
         u[k] += alpha * p[k];
         const double rk = r[k] - alpha * ap[k];
         r[k] = rk;
-        if (b0f) b0f[k] = (float)rk;
+        if (b0f) {  // r as FP32 hi + lo for the FP32 cycle
+            const float hi = (float)rk;
+            b0f[k] = hi;
+            b0lo[k] = (float)(rk - (double)hi);
+        }
         if (zold) acc2 += rk * (double)zold[k];
         acc += rk * rk;
     }
@@ -510,31 +509,30 @@ static inline int tiles_grid(int n) {
 }
 
 template <class T>
-void launch_visit_pre(const Lvl64& H, const T* b, const double* b64, const T* xin, T* xout, T* bc, cudaStream_t s) {
-    if (H.n <= 256)
-        launch_k(k_visit_pre<T, 8, 16>, tiles_grid<8, 16>(H.n), 128, VisitSmem<T, 8, 16>::bytes, s, H, b, b64, xin,
-                 xout, bc);
+void launch_visit_pre(const VisitLevel<T>& V, const T* xin, T* xout, T* bc, cudaStream_t s) {
+    if (V.n <= 256)
+        launch_k(k_visit_pre<T, 8, 16>, tiles_grid<8, 16>(V.n), 128, VisitSmem<T, 8, 16>::bytes, s, V, xin, xout, bc);
     else
-        launch_k(k_visit_pre<T, 16, 32>, tiles_grid<16, 32>(H.n), 256, VisitSmem<T, 16, 32>::bytes, s, H, b, b64,
-                 xin, xout, bc);
+        launch_k(k_visit_pre<T, 16, 32>, tiles_grid<16, 32>(V.n), 256, VisitSmem<T, 16, 32>::bytes, s, V, xin, xout,
+                 bc);
 }
 template <class T>
-void launch_visit_post(const Lvl64& H, const T* b, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
+void launch_visit_post(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
                        double* partials, cudaStream_t s) {
-    if (H.n <= 256)
-        launch_k(k_visit_post<T, 8, 16>, tiles_grid<8, 16>(H.n), 128, PostSmem<T, 8, 16>::bytes, s, H, b, xin, xc,
-                 xout, r, st, partials);
+    if (V.n <= 256)
+        launch_k(k_visit_post<T, 8, 16>, tiles_grid<8, 16>(V.n), 128, PostSmem<T, 8, 16>::bytes, s, V, xin, xc, xout,
+                 r, st, partials);
     else
-        launch_k(k_visit_post<T, 16, 32>, tiles_grid<16, 32>(H.n), 256, PostSmem<T, 16, 32>::bytes, s, H, b, xin, xc,
+        launch_k(k_visit_post<T, 16, 32>, tiles_grid<16, 32>(V.n), 256, PostSmem<T, 16, 32>::bytes, s, V, xin, xc,
                  xout, r, st, partials);
 }
 
 // ------------------------------------------------------------ launch wrappers
 
 void launch_cg_init(const double* f, double h2, int64_t m, double* b, double* r, double* u, double* p,
-                    float* b0f, const double* u0, const Lvl64& L0, CgState* st, double* partials,
+                    float* b0f, float* b0lo, const double* u0, const Lvl64& L0, CgState* st, double* partials,
                     cudaStream_t s) {
-    launch_k(k_cg_init, grid_for(m), kThreads, 0, s, f, h2, m, b, r, u, p, b0f, u0, L0, st, partials);
+    launch_k(k_cg_init, grid_for(m), kThreads, 0, s, f, h2, m, b, r, u, p, b0f, b0lo, u0, L0, st, partials);
 }
 template <class T>
 void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s) {
@@ -589,9 +587,9 @@ void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, 
                       cudaStream_t s) {
     launch_k(k_apply_dot, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, p, ap, st, partials);
 }
-void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, const float* zold,
-                      int64_t m, CgState* st, double* partials, cudaStream_t s) {
-    launch_k(k_cg_update, grid_for(m), kThreads, 0, s, p, ap, u, r, b0f, zold, m, st, partials);
+void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, float* b0lo,
+                      const float* zold, int64_t m, CgState* st, double* partials, cudaStream_t s) {
+    launch_k(k_cg_update, grid_for(m), kThreads, 0, s, p, ap, u, r, b0f, b0lo, zold, m, st, partials);
 }
 void launch_true_residual(const Lvl64& L, const double* u, const double* b, double*, CgState* st,
                           double* partials, cudaStream_t s) {
@@ -611,180 +609,11 @@ void launch_copy_back(const T* src, double* dst, int64_t m, cudaStream_t s) {
 
 // ================================================================ block engine
 
-// Per-CTA layout for one side-n problem. Global arena (L2-resident while the
-// CTA works on the problem): the FP64 hierarchy (e, nf, d, id per level,
-// wb/sb boundary vectors), the five FP64 CG vectors b, r, p, Ap, z, and the
-// cycle's own coefficient copies and iterate/right-hand side for the large
-// levels. Shared memory: the same for every level from `ls` down, as many
-// coarse levels as fit in `sbudget` bytes -- the W-cycle visits level l 2^l
-// times, so the coarse levels are the ones whose latency matters. Level 0 of
-// an FP64 cycle works directly on r (right-hand side) and z (iterate).
-// Shared by host sizing and device carving (gbase/sbase == null: size only).
-struct BlockLayout {
-    size_t global_bytes, smem_bytes;
-    int nlev, ls;
-};
-
-template <class T>
-__host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sbudget, Lvl64* h, Lvl<T>* lv,
-                                      double** cg) {
-    size_t goff = 0, soff = 0;
-    auto gtake = [&](size_t bytes) -> char* {
-        char* ptr = gbase ? gbase + goff : nullptr;
-        goff += (bytes + 255) & ~(size_t)255;
-        return ptr;
-    };
-    auto stake = [&](size_t bytes) -> char* {
-        char* ptr = sbase ? sbase + soff : nullptr;
-        soff += (bytes + 15) & ~(size_t)15;
-        return ptr;
-    };
-    int sides[kMaxLevels];
-    int nlev = 0;
-    for (int s = n; nlev < kMaxLevels;) {
-        sides[nlev++] = s;
-        if (s <= 1) break;
-        s = (s + 1) / 2;
-    }
-    int ls = nlev;
-    size_t need = 0;
-    for (int l = nlev - 1; l >= 1; --l) {
-        const size_t lvl = 6 * (((size_t)sides[l] * sides[l] * sizeof(T) + 15) & ~(size_t)15);
-        if (need + lvl > sbudget) break;
-        need += lvl;
-        ls = l;
-    }
-    const bool fp32 = sizeof(T) == 4;
-    const size_t m0 = (size_t)n * n;
-    for (int l = 0; l < nlev; ++l) {
-        const size_t m = (size_t)sides[l] * sides[l];
-        Lvl64 H;
-        H.n = sides[l];
-        H.e = (double*)gtake(8 * m);
-        H.nf = (double*)gtake(8 * m);
-        H.d = (double*)gtake(8 * m);
-        H.id = (double*)gtake(8 * m);
-        H.wb = (double*)gtake(8 * (size_t)sides[l]);
-        H.sb = (double*)gtake(8 * (size_t)sides[l]);
-        if (h) h[l] = H;
-    }
-    double* v[5];
-    for (int q = 0; q < 5; ++q) v[q] = (double*)gtake(8 * m0);
-    if (cg)
-        for (int q = 0; q < 5; ++q) cg[q] = v[q];
-    for (int l = 0; l < nlev; ++l) {
-        const size_t m = (size_t)sides[l] * sides[l];
-        const bool shared = l >= ls;
-        auto take = [&](size_t bytes) { return shared ? stake(bytes) : gtake(bytes); };
-        Lvl<T> V;
-        V.n = sides[l];
-        if (fp32 || shared) {
-            V.e = (const T*)take(sizeof(T) * m);
-            V.nf = (const T*)take(sizeof(T) * m);
-            V.d = (const T*)take(sizeof(T) * m);
-            V.id = (const T*)take(sizeof(T) * m);
-        } else {
-            V.e = h ? (const T*)h[l].e : nullptr;
-            V.nf = h ? (const T*)h[l].nf : nullptr;
-            V.d = h ? (const T*)h[l].d : nullptr;
-            V.id = h ? (const T*)h[l].id : nullptr;
-        }
-        if (l == 0 && !fp32) {
-            V.x = (T*)v[4];  // z
-            V.b = (T*)v[1];  // r
-        } else {
-            V.x = (T*)take(sizeof(T) * m);
-            V.b = (T*)take(sizeof(T) * m);
-        }
-        if (lv) lv[l] = V;
-    }
-    return BlockLayout{goff, soff, nlev, ls};
-}
-
 int num_levels_for(int n) { return carve<double>(n, nullptr, nullptr, 0, nullptr, nullptr, nullptr).nlev; }
 
 size_t block_arena_bytes(int n, bool mixed, size_t sbudget) {
     return mixed ? carve<float>(n, nullptr, nullptr, sbudget, nullptr, nullptr, nullptr).global_bytes
                  : carve<double>(n, nullptr, nullptr, sbudget, nullptr, nullptr, nullptr).global_bytes;
-}
-
-// Cycle coefficients of level l in the cycle's precision (FP32 copies for the
-// mixed form, shared-memory copies for the levels held on chip).
-template <class T>
-__device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& V) {
-    if ((const void*)V.e == (const void*)H.e) return;  // FP64 level used in place
-    const int64_t m = (int64_t)H.n * H.n;
-    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-        ((T*)V.e)[k] = (T)H.e[k];
-        ((T*)V.nf)[k] = (T)H.nf[k];
-        ((T*)V.d)[k] = (T)H.d[k];
-        ((T*)V.id)[k] = (T)H.id[k];
-    }
-}
-
-// y = A x over a block, FP64, returning sum x . y (or x . x when want_xx).
-__device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* x, double* y, double* red) {
-    const int n = L.n;
-    const int64_t m = (int64_t)n * n;
-    double acc = 0.0;
-    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
-        const double v = apply_cell(L, x, i, j);
-        y[k] = v;
-        acc += x[k] * v;
-    }
-    return block_sum(acc, red);
-}
-
-// z = M r for one problem; returns r . z. For the FP32 cycle, r is rounded
-// into the level-0 right-hand side and the FP32 iterate widened into z.
-template <class T>
-__device__ double block_precondition(const BatchArgs& A, const Lvl64* h, const Lvl<T>* lv, int nlev,
-                                     const double* r, double* z, double* red) {
-    const int n = h[0].n;
-    const int64_t m = (int64_t)n * n;
-    double acc = 0.0;
-    if (A.pc == kPcMultigrid) {
-        if (sizeof(T) == 4) {
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) lv[0].b[k] = (T)r[k];
-            __syncthreads();
-            block_cycle<T>(lv, 0, nlev, A.pre, A.post, A.gamma, 1, h[nlev - 1].id);
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-                const double zk = (double)lv[0].x[k];
-                z[k] = zk;
-                acc += r[k] * zk;
-            }
-        } else {
-            block_cycle<T>(lv, 0, nlev, A.pre, A.post, A.gamma, 1, nullptr);
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) acc += r[k] * z[k];
-        }
-    } else {
-        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-            const double zk = A.pc == kPcJacobi ? r[k] * h[0].id[k] : r[k];
-            z[k] = zk;
-            acc += r[k] * zk;
-        }
-    }
-    return block_sum(acc, red);
-}
-
-// Build the hierarchy of one problem into the CTA's arena. Returns the first
-// invalid permeability index (~0 if the field is valid).
-template <class T>
-__device__ unsigned long long block_setup(const BatchArgs& A, const double* a, const Lvl64* h, const Lvl<T>* lv,
-                                          int nlev, unsigned long long* s_bad) {
-    if (threadIdx.x == 0) *s_bad = ~0ull;
-    __syncthreads();
-    build_fine<BlockScope>(a, h[0], s_bad);
-    __syncthreads();
-    for (int l = 1; l < nlev; ++l) {
-        coarsen<BlockScope>(h[l - 1], h[l]);
-        __syncthreads();
-    }
-    if (A.pc == kPcMultigrid)
-        for (int l = 0; l < nlev; ++l) block_copy_coeffs<T>(h[l], lv[l]);
-    __syncthreads();
-    return *s_bad;
 }
 
 // One whole PCG solve (solver.hpp:83-174) by one CTA.
@@ -996,8 +825,8 @@ void launch_block_precondition(const BatchArgs& args, const double* r, double* z
                                  cudaStream_t);                                                            \
     template void launch_dot_rz<T>(const T*, const double*, int64_t, CgState*, double*, cudaStream_t);     \
     template void launch_tail_matvec<T>(const T*, int, const T*, T*, CgState*, cudaStream_t);              \
-    template void launch_visit_pre<T>(const Lvl64&, const T*, const double*, const T*, T*, T*, cudaStream_t); \
-    template void launch_visit_post<T>(const Lvl64&, const T*, const T*, const T*, T*, const double*,        \
+    template void launch_visit_pre<T>(const VisitLevel<T>&, const T*, T*, T*, cudaStream_t);                 \
+    template void launch_visit_post<T>(const VisitLevel<T>&, const T*, const T*, T*, const double*,          \
                                        CgState*, double*, cudaStream_t);                                   \
     template void launch_xpby<T>(const T*, double*, int64_t, CgState*, cudaStream_t);                      \
     template void launch_copy_cast<T>(const double*, T*, int64_t, cudaStream_t);                           \

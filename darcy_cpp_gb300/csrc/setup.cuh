@@ -79,15 +79,24 @@ __device__ __forceinline__ void coarsen(const Lvl64& F, const Lvl64& C) {
     }
 }
 
-// FP32 copy of a level's coefficients for the mixed-precision cycle.
+// FP32 copy of a level's coefficients for the mixed-precision cycle. When
+// the lo pointers are given, also the rounding remainders of e, nf, d
+// (c - (double)(float)c, rounded to FP32): hi + lo carries ~48 bits.
 template <class S>
-__device__ __forceinline__ void to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id) {
+__device__ __forceinline__ void to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, float* elo,
+                                        float* nlo, float* dlo) {
     const int64_t m = (int64_t)L.n * L.n;
     for (int64_t k = S::start(); k < m; k += S::stride()) {
-        e[k] = (float)L.e[k];
-        nf[k] = (float)L.nf[k];
-        d[k] = (float)L.d[k];
+        const float eh = (float)L.e[k], nh = (float)L.nf[k], dh = (float)L.d[k];
+        e[k] = eh;
+        nf[k] = nh;
+        d[k] = dh;
         id[k] = (float)L.id[k];
+        if (elo) {
+            elo[k] = (float)(L.e[k] - (double)eh);
+            nlo[k] = (float)(L.nf[k] - (double)nh);
+            dlo[k] = (float)(L.d[k] - (double)dh);
+        }
     }
 }
 

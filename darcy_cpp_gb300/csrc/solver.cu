@@ -158,7 +158,8 @@ struct GridPlan {
     Arena arena;
     double *a = nullptr, *f = nullptr, *u0 = nullptr, *u = nullptr;
     double *b = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr;
-    float *x0f = nullptr, *b0f = nullptr;
+    float *x0f = nullptr, *b0f = nullptr, *b0lo = nullptr;
+    std::vector<float*> elo, nlo, dlo;  // FP32 lo parts of the coefficients (mixed form)
     std::vector<Lvl64> h;
     std::vector<Lvl<double>> lvd;
     std::vector<Lvl<float>> lvf;
@@ -248,6 +249,9 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
     P.lvf.assign(P.nlev, Lvl<float>{});
     P.X0.assign(P.nlev, nullptr);
     P.X1.assign(P.nlev, nullptr);
+    P.elo.assign(P.nlev, nullptr);
+    P.nlo.assign(P.nlev, nullptr);
+    P.dlo.assign(P.nlev, nullptr);
     P.fused = K.pre == 1 && K.post == 1;
     auto layout = [&](Carver& A) {
         P.a = A.take<double>(m);
@@ -261,6 +265,7 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
         P.z = A.take<double>(m);
         P.x0f = A.take<float>(m);
         P.b0f = A.take<float>(m);
+        P.b0lo = A.take<float>(m);
         for (int l = 0; l < P.nlev; ++l) {
             const size_t ml = (size_t)sides[l] * sides[l];
             Lvl64& H = P.h[l];
@@ -277,6 +282,9 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
             F.nf = A.take<float>(ml);
             F.d = A.take<float>(ml);
             F.id = A.take<float>(ml);
+            P.elo[l] = A.take<float>(ml);
+            P.nlo[l] = A.take<float>(ml);
+            P.dlo[l] = A.take<float>(ml);
             Lvl<double>& D = P.lvd[l];
             D.n = sides[l];
             D.e = H.e;
@@ -375,6 +383,21 @@ void emit_visit(GridPlan& P, int l, bool first, cudaStream_t s) {
     }
 }
 
+// What the fused visit kernels read for level l: the FP64 hierarchy, or the
+// FP32 hi/lo pairs of the mixed form (with r's lo part on level 0).
+template <class T>
+VisitLevel<T> visit_level(const GridPlan& P, int l);
+template <>
+VisitLevel<double> visit_level<double>(const GridPlan& P, int l) {
+    const Lvl64& H = P.h[l];
+    return VisitLevel<double>{H.n, H.e, H.nf, H.d, H.id, nullptr, nullptr, nullptr, P.lvd[l].b, nullptr};
+}
+template <>
+VisitLevel<float> visit_level<float>(const GridPlan& P, int l) {
+    const Lvl<float>& F = P.lvf[l];
+    return VisitLevel<float>{F.n, F.e, F.nf, F.d, F.id, P.elo[l], P.nlo[l], P.dlo[l], F.b, l == 0 ? P.b0lo : nullptr};
+}
+
 // Fused visit (pre_sweeps = post_sweeps = 1): two kernels per level visit,
 // iterates alternating between the level's two buffers. `cur` tracks which
 // buffer holds each level's iterate while the host walks the recursion.
@@ -383,15 +406,12 @@ void emit_visit_fused(GridPlan& P, int l, bool first, std::vector<int>& cur, cud
     const auto& lv = levels_of<T>(P);
     const PlanKey& K = P.key;
     auto X = [&](int lvl, int q) { return (T*)(q == 0 ? P.X0[lvl] : P.X1[lvl]); };
-    const Lvl<T>& A = lv[l];
-    const Lvl64& H = P.h[l];
-    // level 0 of the FP32 cycle restricts the residual of the exact FP64 r
-    const double* b64 = (l == 0 && sizeof(T) == 4) ? P.r : nullptr;
+    const VisitLevel<T> V = visit_level<T>(P, l);
     if (first) {
-        launch_visit_pre<T>(H, A.b, b64, nullptr, X(l, 0), lv[l + 1].b, s);
+        launch_visit_pre<T>(V, nullptr, X(l, 0), lv[l + 1].b, s);
         cur[l] = 0;
     } else {
-        launch_visit_pre<T>(H, A.b, b64, X(l, cur[l]), X(l, cur[l] ^ 1), lv[l + 1].b, s);
+        launch_visit_pre<T>(V, X(l, cur[l]), X(l, cur[l] ^ 1), lv[l + 1].b, s);
         cur[l] ^= 1;
     }
     if (l + 1 >= P.tail_l0) {
@@ -400,7 +420,7 @@ void emit_visit_fused(GridPlan& P, int l, bool first, std::vector<int>& cur, cud
     } else {
         for (int g = 0; g < K.gamma; ++g) emit_visit_fused<T>(P, l + 1, g == 0, cur, s);
     }
-    launch_visit_post<T>(H, A.b, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1), l == 0 ? P.r : nullptr, P.st,
+    launch_visit_post<T>(V, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1), l == 0 ? P.r : nullptr, P.st,
                          P.partials, s);
     cur[l] ^= 1;
 }
@@ -411,7 +431,7 @@ void emit_setup(GridPlan& P, cudaStream_t s) {
     if (P.mixed_mg)
         for (int l = 0; l < P.nlev; ++l)
             launch_to_fp32(P.h[l], (float*)P.lvf[l].e, (float*)P.lvf[l].nf, (float*)P.lvf[l].d,
-                           (float*)P.lvf[l].id, s);
+                           (float*)P.lvf[l].id, P.elo[l], P.nlo[l], P.dlo[l], s);
     if (P.key.pc == kPcMultigrid) {
         // The tail operator is built in FP64 (Galerkin levels and the exact
         // coarsest solve inside it stay FP64) and rounded once for the mixed form.
@@ -453,7 +473,7 @@ void emit_prologue(GridPlan& P, cudaStream_t s) {
     const double hh = 1.0 / (double)(P.n + 1);
     emit_setup(P, s);
     launch_cg_init(P.key.has_f ? P.f : nullptr, hh * hh, P.m, P.b, P.r, P.u, P.p, P.mixed_mg ? P.b0f : nullptr,
-                   P.key.has_u0 ? P.u0 : nullptr, P.h[0], P.st, P.partials, s);
+                   P.b0lo, P.key.has_u0 ? P.u0 : nullptr, P.h[0], P.st, P.partials, s);
     emit_precondition(P, s);
 }
 
@@ -466,7 +486,7 @@ void emit_body(GridPlan& P, cudaStream_t s) {
     // Standard beta in both forms: the flexible (Polak-Ribiere) beta that
     // k_cg_update supports measured worse for the FP32 cycle (1024^2 at 1e6
     // contrast: 127 iterations against 114 with the standard beta).
-    launch_cg_update(P.p, P.ap, P.u, P.r, P.mixed_mg ? P.b0f : nullptr, nullptr, P.m, P.st, P.partials, s);
+    launch_cg_update(P.p, P.ap, P.u, P.r, P.mixed_mg ? P.b0f : nullptr, P.b0lo, nullptr, P.m, P.st, P.partials, s);
     emit_precondition(P, s);
 }
 
@@ -1302,15 +1322,15 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
             const T* Tm = tail_matrix<T>(P);
             // algorithmic bytes: every array the kernel must touch, once
             if (P.fused) {
-                const Lvl64 H0 = P.h[0];
+                const VisitLevel<T> V0 = visit_level<T>(P, 0);
                 T* xa = (T*)P.X0[0];
                 T* xb = (T*)P.X1[0];
                 T* x1 = (T*)P.X0[1];
-                const double* b64 = sizeof(T) == 4 ? rvec : nullptr;
-                items.push_back({"visit_pre(l0)", 32 * m + w * (2 * m + mc) + (b64 ? 8 * m : 0), 1.0,
-                                 [=] { launch_visit_pre<T>(H0, L0.b, b64, nullptr, xa, L1.b, s); }});
-                items.push_back({"visit_post(l0)", 24 * m + w * (3 * m + mc) + 8 * m, 1.0, [=] {
-                                     launch_visit_post<T>(H0, L0.b, xa, x1, xb, rvec, stp, partials, s);
+                const double cb = sizeof(T) == 4 ? 7 * 4.0 : 4 * 8.0;  // staged coefficient bytes per cell
+                items.push_back({"visit_pre(l0)", cb * m + w * (2 * m + mc) + (sizeof(T) == 4 ? 4 * m : 0), 1.0,
+                                 [=] { launch_visit_pre<T>(V0, nullptr, xa, L1.b, s); }});
+                items.push_back({"visit_post(l0)", 3 * w * m + w * (3 * m + mc) + 8 * m, 1.0, [=] {
+                                     launch_visit_post<T>(V0, xa, x1, xb, rvec, stp, partials, s);
                                  }});
             }
             items.push_back({"gs_colour0_zero(l0)", w * m * 1.5, 1.0, [=] { launch_gs<T>(L0, 0, true, stp, s); }});
@@ -1337,6 +1357,7 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
         double* const rw = P.r;
         float* const x0f = P.x0f;
         float* const b0f = P.b0f;
+        float* const b0lo = P.b0lo;
         const double* const zv = P.z;
         if (f32)
             items.push_back({"xpby", (4 + 16) * m, 1.0, [=] { launch_xpby<float>(x0f, pv, mm, stp, s); }});
@@ -1344,8 +1365,8 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
             items.push_back({"xpby", 24 * m, 1.0, [=] { launch_xpby<double>(zv, pv, mm, stp, s); }});
         items.push_back({"apply_dot", 40 * m, 1.0, [=] { launch_apply_dot(H0, pv, apv, stp, partials, s); }});
         items.push_back({"cg_update", (48 + (f32 ? 8 : 0)) * m, 1.0, [=] {
-                             launch_cg_update(pv, apv, uv, rw, f32 ? b0f : nullptr, f32 ? x0f : nullptr, mm, stp,
-                                              partials, s);
+                             launch_cg_update(pv, apv, uv, rw, f32 ? b0f : nullptr, b0lo, nullptr, mm, stp, partials,
+                                              s);
                          }});
         int q = 0;
         for (const Item& it : items) {
