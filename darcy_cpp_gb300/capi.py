@@ -77,6 +77,8 @@ def lib() -> ctypes.CDLL:
         L.dgpu_profile_kernels.argtypes = [_P, _P, ctypes.c_int64, ctypes.POINTER(Options), ctypes.c_int,
                                            ctypes.POINTER(KernelTime), ctypes.c_int, _I]
         L.dgpu_flush_l2.argtypes = [_P, ctypes.c_int64]
+        L.dgpu_apply_preconditioner_noalloc.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                                        ctypes.c_int, _P, _P]
         _lib = L
     return _lib
 
@@ -102,6 +104,15 @@ def _ptr(arr: np.ndarray | None):
 
 def _f64(x) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+
+
+def apply_preconditioner_noalloc(d_a: int, d_r: int, n: int, d_z: int, pre_sweeps: int = 1, post_sweeps: int = 1,
+                                 cycle_index: int = 2, stream: int | None = None) -> None:
+    """z = M r on caller-owned device buffers with no device allocation
+    (dgpu_apply_preconditioner_noalloc; n <= 128, calls must not overlap)."""
+    check(lib().dgpu_apply_preconditioner_noalloc(ctypes.c_void_p(d_a), ctypes.c_void_p(d_r), int(n), int(pre_sweeps),
+                                                  int(post_sweeps), int(cycle_index), ctypes.c_void_p(d_z),
+                                                  ctypes.c_void_p(stream) if stream else None))
 
 
 class Context:

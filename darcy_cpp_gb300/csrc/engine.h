@@ -82,6 +82,9 @@ inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 size_t block_arena_bytes(int n, bool mixed, size_t smem_budget);
 int num_levels_for(int n);
 
+// Message returned by dgpu_last_error() on this thread (solver.cu).
+void set_last_error(const char* msg);
+
 // Programmatic dependent launch for the grid engine's kernels (on by
 // default; DARCY_GPU_PDL=0 turns it off).
 void set_programmatic_launch(bool on);

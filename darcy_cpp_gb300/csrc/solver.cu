@@ -1028,6 +1028,8 @@ void grid_precondition(dgpu_context* C, const double* a, const double* r, int64_
 
 }  // namespace
 
+void dgpu::set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
 extern "C" {
 
 const char* dgpu_last_error(void) { return g_err.c_str(); }

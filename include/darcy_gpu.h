@@ -142,6 +142,22 @@ int dgpu_num_levels(int64_t n);
 int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dgpu_options* opt, int reps,
                          dgpu_kernel_time* out, int cap, int* count);
 
+/* Allocation-free z = M r (one multigrid cycle from a zero guess) for callers
+ * that cannot allocate device memory while they run -- code inside a host
+ * that owns all device memory itself (a serving pool, a framework allocator)
+ * or a loop that must not enter cudaMalloc/cudaFree, which can synchronise
+ * the device. No counterpart in the reference. The caller passes device
+ * buffers a, r, z (n*n doubles each) and an optional cudaStream_t; the
+ * scratch is a fixed 2 MiB array inside the library, present on every device
+ * that loads it until the process exits, so n is limited to 1..128 (larger n
+ * returns DGPU_INVALID_INPUT). No context is needed and nothing is allocated:
+ * the first call on a device looks up the array's device address (make that
+ * first call outside any stream capture). All calls share the one array, so
+ * calls that overlap on the GPU race; serialise them. Blocks until z is
+ * written (it reads back a status word to report invalid permeability). */
+int dgpu_apply_preconditioner_noalloc(const double* d_a, const double* d_r, int64_t n, int pre_sweeps,
+                                      int post_sweeps, int cycle_index, double* d_z, void* stream);
+
 /* Write `bytes` of device memory on the context stream (evicts L2 between
  * timed runs). */
 int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes);
