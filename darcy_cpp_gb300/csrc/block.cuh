@@ -25,21 +25,39 @@ __device__ __forceinline__ double apply_cell(const Lvl64& L, const double* __res
 
 // Per-CTA layout for one side-n problem. Global arena (L2-resident while the
 // CTA works on the problem): the FP64 hierarchy (e, nf, d, id per level,
-// wb/sb boundary vectors), the five FP64 CG vectors b, r, p, Ap, z, and the
+// wb/sb boundary vectors), the five FP64 CG vectors b, r, p, Ap, z, the
 // cycle's own coefficient copies and iterate/right-hand side for the large
-// levels. Shared memory: the same for every level from `ls` down, as many
-// coarse levels as fit in `sbudget` bytes -- the W-cycle visits level l 2^l
-// times, so the coarse levels are the ones whose latency matters. Level 0 of
-// an FP64 cycle works directly on r (right-hand side) and z (iterate).
+// levels, and the scratch used once per problem to build the dense tail.
+// Shared memory: the dense tail operator, then the cycle's data for as many
+// coarse levels as fit in `sbudget` bytes. Level 0 of an FP64 cycle works
+// directly on r (right-hand side) and z (iterate).
+//
+// Dense tail: the levels from tl (the first level of side <= kBlockTailSide,
+// when that is not level 0) down implement the fixed map "x = 0, then gamma
+// cycles"; it is built once per problem as an N x N matrix (N = side_tl^2,
+// one column per unit right-hand side, all columns at once) and the cycle
+// applies it with one product per visit of level tl - 1 instead of visiting
+// 2^k levels below. Same operator as the recursion, to rounding.
 // Shared by host sizing and device carving (gbase/sbase == null: size only).
+constexpr int kBlockTailSide = 8;
+
 struct BlockLayout {
     size_t global_bytes, smem_bytes;
     int nlev, ls;
 };
 
 template <class T>
-__host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sbudget, Lvl64* h, Lvl<T>* lv,
-                                      double** cg) {
+struct BlockViews {
+    Lvl64 h[kMaxLevels];        // FP64 hierarchy
+    Lvl<T> lv[kMaxLevels];      // the cycle's levels
+    Lvl<double> lm[kMaxLevels]; // tail construction: FP64 levels with N right-hand sides
+    double* cg[5];              // b, r, p, Ap, z
+    T* tail;                    // dense tail operator (ntail x ntail), or null
+    int nlev, tl, ntail;
+};
+
+template <class T>
+__host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sbudget, BlockViews<T>* v) {
     size_t goff = 0, soff = 0;
     auto gtake = [&](size_t bytes) -> char* {
         char* ptr = gbase ? gbase + goff : nullptr;
@@ -58,13 +76,38 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
         if (s <= 1) break;
         s = (s + 1) / 2;
     }
-    int ls = nlev;
-    size_t need = 0;
-    for (int l = nlev - 1; l >= 1; --l) {
+    int tl = 0;
+    for (int l = 1; l < nlev; ++l)
+        if (sides[l] <= kBlockTailSide) {
+            tl = l;
+            break;
+        }
+    const int ntail = tl ? sides[tl] * sides[tl] : 0;
+    const int cyc_levels = tl ? tl : nlev;  // levels the cycle itself visits
+    // shared memory: the tail operator first, then the coarsest cycle levels that fit
+    // (the operator plus level tl's x and b, which it reads and writes)
+    size_t need = tl ? (((size_t)ntail * ntail * sizeof(T) + 15) & ~(size_t)15) +
+                           2 * (((size_t)ntail * sizeof(T) + 15) & ~(size_t)15)
+                     : 0;
+    const bool tail_shared = tl && need <= sbudget;
+    if (!tail_shared) need = 0;
+    int ls = cyc_levels;
+    for (int l = cyc_levels - 1; l >= 1; --l) {
         const size_t lvl = 6 * (((size_t)sides[l] * sides[l] * sizeof(T) + 15) & ~(size_t)15);
         if (need + lvl > sbudget) break;
         need += lvl;
         ls = l;
+    }
+    if (v) {
+        v->nlev = nlev;
+        v->tl = tl;
+        v->ntail = ntail;
+        v->tail = nullptr;
+    }
+    if (tl) {
+        T* tp = (T*)(tail_shared ? stake(sizeof(T) * (size_t)ntail * ntail)
+                                 : gtake(sizeof(T) * (size_t)ntail * ntail));
+        if (v) v->tail = tp;
     }
     const bool fp32 = sizeof(T) == 4;
     const size_t m0 = (size_t)n * n;
@@ -78,37 +121,60 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
         H.id = (double*)gtake(8 * m);
         H.wb = (double*)gtake(8 * (size_t)sides[l]);
         H.sb = (double*)gtake(8 * (size_t)sides[l]);
-        if (h) h[l] = H;
+        if (v) v->h[l] = H;
     }
-    double* v[5];
-    for (int q = 0; q < 5; ++q) v[q] = (double*)gtake(8 * m0);
-    if (cg)
-        for (int q = 0; q < 5; ++q) cg[q] = v[q];
+    double* cgv[5];
+    for (int q = 0; q < 5; ++q) cgv[q] = (double*)gtake(8 * m0);
+    if (v)
+        for (int q = 0; q < 5; ++q) v->cg[q] = cgv[q];
     for (int l = 0; l < nlev; ++l) {
         const size_t m = (size_t)sides[l] * sides[l];
-        const bool shared = l >= ls;
-        auto take = [&](size_t bytes) { return shared ? stake(bytes) : gtake(bytes); };
-        Lvl<T> V;
+        Lvl<T> V{};
         V.n = sides[l];
-        if (fp32 || shared) {
-            V.e = (const T*)take(sizeof(T) * m);
-            V.nf = (const T*)take(sizeof(T) * m);
-            V.d = (const T*)take(sizeof(T) * m);
-            V.id = (const T*)take(sizeof(T) * m);
-        } else {
-            V.e = h ? (const T*)h[l].e : nullptr;
-            V.nf = h ? (const T*)h[l].nf : nullptr;
-            V.d = h ? (const T*)h[l].d : nullptr;
-            V.id = h ? (const T*)h[l].id : nullptr;
+        if (tl && l > tl) {  // inside the tail: never visited by the cycle
+            if (v) v->lv[l] = V;
+            continue;
+        }
+        const bool shared = (l >= ls && l < cyc_levels) || (tail_shared && l == tl);
+        auto take = [&](size_t bytes) { return shared ? stake(bytes) : gtake(bytes); };
+        if (l < cyc_levels) {
+            if (fp32 || shared) {
+                V.e = (const T*)take(sizeof(T) * m);
+                V.nf = (const T*)take(sizeof(T) * m);
+                V.d = (const T*)take(sizeof(T) * m);
+                V.id = (const T*)take(sizeof(T) * m);
+            } else if (v) {
+                V.e = (const T*)v->h[l].e;
+                V.nf = (const T*)v->h[l].nf;
+                V.d = (const T*)v->h[l].d;
+                V.id = (const T*)v->h[l].id;
+            }
         }
         if (l == 0 && !fp32) {
-            V.x = (T*)v[4];  // z
-            V.b = (T*)v[1];  // r
+            V.x = (T*)cgv[4];  // z
+            V.b = (T*)cgv[1];  // r
         } else {
+            // level tl (the tail's input/output) only needs x and b
             V.x = (T*)take(sizeof(T) * m);
             V.b = (T*)take(sizeof(T) * m);
         }
-        if (lv) lv[l] = V;
+        if (v) v->lv[l] = V;
+    }
+    if (tl) {  // tail construction scratch: every tail level with ntail right-hand sides
+        for (int l = tl; l < nlev; ++l) {
+            const size_t m = (size_t)sides[l] * sides[l];
+            Lvl<double> M{};
+            M.n = sides[l];
+            M.x = (double*)gtake(8 * m * ntail);
+            M.b = (double*)gtake(8 * m * ntail);
+            if (v) {
+                M.e = v->h[l].e;
+                M.nf = v->h[l].nf;
+                M.d = v->h[l].d;
+                M.id = v->h[l].id;
+                v->lm[l] = M;
+            }
+        }
     }
     return BlockLayout{goff, soff, nlev, ls};
 }
@@ -117,7 +183,7 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
 // mixed form, shared-memory copies for the levels held on chip).
 template <class T>
 __device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& V) {
-    if ((const void*)V.e == (const void*)H.e) return;  // FP64 level used in place
+    if (!V.e || (const void*)V.e == (const void*)H.e) return;  // not visited / FP64 used in place
     const int64_t m = (int64_t)H.n * H.n;
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
         ((T*)V.e)[k] = (T)H.e[k];
@@ -127,7 +193,7 @@ __device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& 
     }
 }
 
-// y = A x over a block, FP64, returning sum x . y (or x . x when want_xx).
+// y = A x over a block, FP64, returning sum x . y.
 __device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* x, double* y, double* red) {
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
@@ -144,28 +210,29 @@ __device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* 
 // z = M r for one problem; returns r . z. For the FP32 cycle, r is rounded
 // into the level-0 right-hand side and the FP32 iterate widened into z.
 template <class T>
-__device__ double block_precondition(const BatchArgs& A, const Lvl64* h, const Lvl<T>* lv, int nlev,
-                                     const double* r, double* z, double* red) {
-    const int n = h[0].n;
+__device__ double block_precondition(const BatchArgs& A, const BlockViews<T>& V, const double* r, double* z,
+                                     double* red) {
+    const int n = V.h[0].n;
     const int64_t m = (int64_t)n * n;
     double acc = 0.0;
     if (A.pc == kPcMultigrid) {
+        const double* id64 = V.h[V.nlev - 1].id;  // FP64 exact coarsest solve (no-tail hierarchies)
         if (sizeof(T) == 4) {
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) lv[0].b[k] = (T)r[k];
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) V.lv[0].b[k] = (T)r[k];
             __syncthreads();
-            block_cycle<T>(lv, 0, nlev, A.pre, A.post, A.gamma, 1, h[nlev - 1].id);
+            block_cycle<T>(V.lv, 0, V.nlev, A.pre, A.post, A.gamma, 1, id64, V.tail, V.tl);
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-                const double zk = (double)lv[0].x[k];
+                const double zk = (double)V.lv[0].x[k];
                 z[k] = zk;
                 acc += r[k] * zk;
             }
         } else {
-            block_cycle<T>(lv, 0, nlev, A.pre, A.post, A.gamma, 1, nullptr);
+            block_cycle<T>(V.lv, 0, V.nlev, A.pre, A.post, A.gamma, 1, nullptr, V.tail, V.tl);
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) acc += r[k] * z[k];
         }
     } else {
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-            const double zk = A.pc == kPcJacobi ? r[k] * h[0].id[k] : r[k];
+            const double zk = A.pc == kPcJacobi ? r[k] * V.h[0].id[k] : r[k];
             z[k] = zk;
             acc += r[k] * zk;
         }
@@ -173,21 +240,44 @@ __device__ double block_precondition(const BatchArgs& A, const Lvl64* h, const L
     return block_sum(acc, red);
 }
 
-// Build the hierarchy of one problem into the CTA's arena. Returns the first
-// invalid permeability index (~0 if the field is valid).
+// The dense tail of one problem: column j = the tail map applied to e_j, all
+// columns at once in FP64 on the FP64 hierarchy, then stored (rounded for the
+// FP32 cycle) row-major.
 template <class T>
-__device__ unsigned long long block_setup(const BatchArgs& A, const double* a, const Lvl64* h, const Lvl<T>* lv,
-                                          int nlev, unsigned long long* s_bad) {
+__device__ void block_build_tail(const BatchArgs& A, const BlockViews<T>& V) {
+    const int tl = V.tl, N = V.ntail;
+    const Lvl<double>& L = V.lm[tl];
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+        const int j = t / N, k = t - j * N;  // right-hand side j, cell k
+        L.b[t] = (k == j) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    block_cycle_m<double>(V.lm, tl, V.nlev, A.pre, A.post, A.gamma, A.gamma, N);
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+        const int j = t / N, k = t - j * N;
+        V.tail[k * N + j] = (T)L.x[t];
+    }
+    __syncthreads();
+}
+
+// Build the hierarchy of one problem into the CTA's arena (and its dense
+// tail). Returns the first invalid permeability index (~0 if valid).
+template <class T>
+__device__ unsigned long long block_setup(const BatchArgs& A, const double* a, const BlockViews<T>& V,
+                                          unsigned long long* s_bad) {
     if (threadIdx.x == 0) *s_bad = ~0ull;
     __syncthreads();
-    build_fine<BlockScope>(a, h[0], s_bad);
+    build_fine<BlockScope>(a, V.h[0], s_bad);
     __syncthreads();
-    for (int l = 1; l < nlev; ++l) {
-        coarsen<BlockScope>(h[l - 1], h[l]);
+    for (int l = 1; l < V.nlev; ++l) {
+        coarsen<BlockScope>(V.h[l - 1], V.h[l]);
         __syncthreads();
     }
-    if (A.pc == kPcMultigrid)
-        for (int l = 0; l < nlev; ++l) block_copy_coeffs<T>(h[l], lv[l]);
+    if (A.pc == kPcMultigrid) {
+        for (int l = 0; l < V.nlev; ++l) block_copy_coeffs<T>(V.h[l], V.lv[l]);
+        __syncthreads();
+        if (V.tl && *s_bad == ~0ull) block_build_tail<T>(A, V);
+    }
     __syncthreads();
     return *s_bad;
 }

@@ -145,8 +145,6 @@ template <class T>
 void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream_t s);
 template <class T>
 int block_solve_occupancy(int threads, size_t smem);
-// Block-engine preconditioner only: z = M r for one problem (apply_preconditioner hook).
-template <class T>
-void launch_block_precondition(const BatchArgs& args, const double* r, double* z, int threads, cudaStream_t s);
+
 
 }  // namespace dgpu

@@ -13,8 +13,10 @@
 // (x = 0 and face = 0), which reproduces the reference's skipped boundary
 // terms exactly: adding e * 0 leaves the running sum bit-identical.
 //
-// Coefficients do not change during a solve, so they are staged before the
-// programmatic-launch wait and their load overlaps the previous kernel.
+// Coefficients do not change during a solve (they are written by the setup
+// kernels, which complete before the solve's loop starts), so they are
+// staged before the programmatic-launch wait and their load overlaps the
+// previous kernel; everything the previous kernel produces is read after it.
 //
 // FP32 cycle (mixed form). Smoothing and transfers run in FP32. The residual
 // that is restricted is formed in double-float arithmetic -- FP32 hi/lo
@@ -200,7 +202,7 @@ __global__ void __launch_bounds__(256) k_visit_pre(VisitLevel<T> V, const T* __r
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int ti0 = (tile / tiles_x) * TH, tj0 = (tile % tiles_x) * TW;
         stage_coeffs<T, TH, TW, R, true, LO>(V, ti0, tj0, es, ns, ds, is, elo, nlo, dlo);
-        if (!waited) {  // coefficients are constant: fetched while the predecessor finishes
+        if (!waited) {
             pdl_enter();
             waited = true;
         }

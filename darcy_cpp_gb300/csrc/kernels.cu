@@ -560,8 +560,7 @@ void launch_tail_columns(const Lvl64* h_dev, const Lvl64* h_host, int l0, int nl
                          int top_calls, int N, double* Td, float* Tf, cudaStream_t s) {
     size_t smem = 0;
     for (int l = l0; l < nlev; ++l) smem += 2 * sizeof(double) * (size_t)h_host[l].n * h_host[l].n;
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_tail_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_tail_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     launch_k(k_tail_columns, N, 256, smem, s, h_dev, l0, nlev, pre, post, gamma, top_calls, N, Td, Tf);
 }
 template <class T>
@@ -609,24 +608,26 @@ void launch_copy_back(const T* src, double* dst, int64_t m, cudaStream_t s) {
 
 // ================================================================ block engine
 
-int num_levels_for(int n) { return carve<double>(n, nullptr, nullptr, 0, nullptr, nullptr, nullptr).nlev; }
+int num_levels_for(int n) { return carve<double>(n, nullptr, nullptr, 0, nullptr).nlev; }
 
 size_t block_arena_bytes(int n, bool mixed, size_t sbudget) {
-    return mixed ? carve<float>(n, nullptr, nullptr, sbudget, nullptr, nullptr, nullptr).global_bytes
-                 : carve<double>(n, nullptr, nullptr, sbudget, nullptr, nullptr, nullptr).global_bytes;
+    return mixed ? carve<float>(n, nullptr, nullptr, sbudget, nullptr).global_bytes
+                 : carve<double>(n, nullptr, nullptr, sbudget, nullptr).global_bytes;
 }
 
 // One whole PCG solve (solver.hpp:83-174) by one CTA.
 template <class T>
-__device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, const Lvl<T>* lv, int nlev,
-                                double* const* cg, double* red, unsigned long long* s_bad) {
+__device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>& V, double* red,
+                                unsigned long long* s_bad) {
     const int n = A.side[pid];
     const int64_t m = (int64_t)n * n;
     const int64_t off = A.off[pid];
     double* u = A.u + off;
-    double *b = cg[0], *r = cg[1], *p = cg[2], *ap = cg[3], *z = cg[4];
+    double *b = V.cg[0], *r = V.cg[1], *p = V.cg[2], *ap = V.cg[3], *z = V.cg[4];
+    const Lvl64* h = V.h;
+    const int nlev = V.nlev;
 
-    const unsigned long long bad = block_setup<T>(A, A.a + off, h, lv, nlev, s_bad);
+    const unsigned long long bad = block_setup<T>(A, A.a + off, V, s_bad);
     if (bad != ~0ull) {
         if (threadIdx.x == 0) {
             A.bad[pid] = bad;
@@ -690,7 +691,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, con
     if (residual < A.tol) {
         converged = 1;
     } else {
-        double rz = block_precondition<T>(A, h, lv, nlev, r, z, red);
+        double rz = block_precondition<T>(A, V, r, z, red);
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k];
         __syncthreads();
         for (int it = 0; it < A.max_iter; ++it) {
@@ -717,7 +718,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, con
                 converged = 1;
                 break;
             }
-            const double rz_new = block_precondition<T>(A, h, lv, nlev, r, z, red);
+            const double rz_new = block_precondition<T>(A, V, r, z, red);
             const double beta = (rz_new - rzo) / rz;
             rz = rz_new;
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k] + beta * p[k];
@@ -746,11 +747,9 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const Lvl64* h, con
 
 template <class T>
 __global__ void __launch_bounds__(1024) k_block_solve(BatchArgs A) {
-    __shared__ Lvl64 h[kMaxLevels];
-    __shared__ Lvl<T> lv[kMaxLevels];
-    __shared__ double* cg[5];
+    __shared__ BlockViews<T> V;
     __shared__ double red[32];
-    __shared__ int s_pid, s_nlev;
+    __shared__ int s_pid;
     __shared__ unsigned long long s_bad;
     extern __shared__ __align__(16) unsigned char block_smem[];
     char* arena = A.scratch + (size_t)blockIdx.x * A.scratch_stride;
@@ -758,60 +757,28 @@ __global__ void __launch_bounds__(1024) k_block_solve(BatchArgs A) {
         if (threadIdx.x == 0) {
             const unsigned w = atomicAdd(A.work, 1u);
             s_pid = w < (unsigned)A.count ? A.order[w] : -1;
-            if (s_pid >= 0)
-                s_nlev = carve<T>(A.side[s_pid], arena, (char*)block_smem, A.smem_budget, h, lv, cg).nlev;
+            if (s_pid >= 0) carve<T>(A.side[s_pid], arena, (char*)block_smem, A.smem_budget, &V);
         }
         __syncthreads();
         const int pid = s_pid;
         if (pid < 0) return;
-        block_solve_one<T>(A, pid, h, lv, s_nlev, cg, red, &s_bad);
+        block_solve_one<T>(A, pid, V, red, &s_bad);
         __syncthreads();
     }
 }
 
-// apply_preconditioner hook: hierarchy of problem 0, then z = M r once.
-template <class T>
-__global__ void __launch_bounds__(1024) k_block_precondition(BatchArgs A, const double* r, double* z) {
-    __shared__ Lvl64 h[kMaxLevels];
-    __shared__ Lvl<T> lv[kMaxLevels];
-    __shared__ double* cg[5];
-    __shared__ double red[32];
-    __shared__ int s_nlev;
-    __shared__ unsigned long long s_bad;
-    extern __shared__ __align__(16) unsigned char block_smem[];
-    if (threadIdx.x == 0) s_nlev = carve<T>(A.side[0], A.scratch, (char*)block_smem, A.smem_budget, h, lv, cg).nlev;
-    __syncthreads();
-    const unsigned long long bad = block_setup<T>(A, A.a, h, lv, s_nlev, &s_bad);
-    if (threadIdx.x == 0) A.bad[0] = bad;
-    if (bad != ~0ull) return;
-    const int64_t m = (int64_t)A.side[0] * A.side[0];
-    double* rr = cg[1];
-    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) rr[k] = r[k];
-    __syncthreads();
-    block_precondition<T>(A, h, lv, s_nlev, rr, cg[4], red);
-    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) z[k] = cg[4][k];
-}
-
 template <class T>
 int block_solve_occupancy(int threads, size_t smem) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // static + dynamic shared memory above 48 KiB needs the opt-in, so set it always
+    cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_block_solve<T>, threads, smem) != cudaSuccess) n = 1;
     return n;
 }
 template <class T>
 void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream_t s) {
-    if (args.smem_budget > 48 * 1024)
-        cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)args.smem_budget);
+    cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)args.smem_budget);
     k_block_solve<T><<<ctas, threads, args.smem_budget, s>>>(args);
-}
-template <class T>
-void launch_block_precondition(const BatchArgs& args, const double* r, double* z, int threads, cudaStream_t s) {
-    if (args.smem_budget > 48 * 1024)
-        cudaFuncSetAttribute(k_block_precondition<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)args.smem_budget);
-    k_block_precondition<T><<<1, threads, args.smem_budget, s>>>(args, r, z);
 }
 
 // ------------------------------------------------------ explicit instantiation
@@ -833,7 +800,7 @@ void launch_block_precondition(const BatchArgs& args, const double* r, double* z
     template void launch_copy_back<T>(const T*, double*, int64_t, cudaStream_t);                           \
     template void launch_block_solve<T>(const BatchArgs&, int, int, cudaStream_t);                          \
     template int block_solve_occupancy<T>(int, size_t);                                                    \
-    template void launch_block_precondition<T>(const BatchArgs&, const double*, double*, int, cudaStream_t);
+
 
 DGPU_INSTANTIATE(double)
 DGPU_INSTANTIATE(float)

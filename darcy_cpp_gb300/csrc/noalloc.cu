@@ -47,29 +47,26 @@ void* g_scratch_addr[kMaxDevices] = {};
 __global__ void __launch_bounds__(256) k_precondition_noalloc(unsigned char* scratch, int n, int pre, int post,
                                                                int gamma, const double* __restrict__ a,
                                                                const double* __restrict__ r, double* __restrict__ z) {
-    __shared__ Lvl64 h[kMaxLevels];
-    __shared__ Lvl<double> lv[kMaxLevels];
-    __shared__ double* cg[5];
+    __shared__ BlockViews<double> V;
     __shared__ double red[32];
-    __shared__ int s_nlev;
     __shared__ unsigned long long s_bad;
-    if (threadIdx.x == 0) s_nlev = carve<double>(n, (char*)scratch, nullptr, 0, h, lv, cg).nlev;
+    if (threadIdx.x == 0) carve<double>(n, (char*)scratch, nullptr, 0, &V);
     __syncthreads();
     BatchArgs A{};
     A.pc = kPcMultigrid;
     A.pre = pre;
     A.post = post;
     A.gamma = gamma;
-    const unsigned long long bad = block_setup<double>(A, a, h, lv, s_nlev, &s_bad);
+    const unsigned long long bad = block_setup<double>(A, a, V, &s_bad);
     unsigned long long* status = reinterpret_cast<unsigned long long*>(scratch + kStatusOffset);
     if (threadIdx.x == 0) *status = bad;
     if (bad != ~0ull) return;
     const int64_t m = (int64_t)n * n;
-    double* rr = cg[1];
+    double* rr = V.cg[1];
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) rr[k] = r[k];
     __syncthreads();
-    block_precondition<double>(A, h, lv, s_nlev, rr, cg[4], red);
-    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) z[k] = cg[4][k];
+    block_precondition<double>(A, V, rr, V.cg[4], red);
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) z[k] = V.cg[4][k];
 }
 
 // Device address of the scratch array on the current device, looked up the
@@ -119,7 +116,7 @@ extern "C" int dgpu_apply_preconditioner_noalloc(const double* d_a, const double
         set_last_error("cycle_index must be 1 or 2");
         return DGPU_INVALID_INPUT;
     }
-    const size_t need = carve<double>((int)n, nullptr, nullptr, 0, nullptr, nullptr, nullptr).global_bytes;
+    const size_t need = carve<double>((int)n, nullptr, nullptr, 0, nullptr).global_bytes;
     if (need > kStatusOffset) {  // cannot happen for n <= kNoAllocMaxSide; kept as the invariant
         set_last_error("allocation-free scratch too small for this grid");
         return DGPU_INVALID_INPUT;

@@ -763,7 +763,10 @@ void save_tuning(dgpu_context* C) {
     std::fclose(fp);
 }
 
-size_t smem_budget_for(bool mixed) { return mixed ? 40 * 1024 : 68 * 1024; }
+// Shared memory for the batched engine's coarse levels and dense tail: sized
+// so that a 64^2 problem keeps levels 32^2 and 16^2 and its 64 x 64 tail on
+// chip with two CTAs per SM.
+size_t smem_budget_for(bool mixed) { return mixed ? 48 * 1024 : 96 * 1024; }
 
 // Packed problems through the block engine. sides/off on the host; a, f, u0
 // host (or device when device_ptrs) packed arrays.

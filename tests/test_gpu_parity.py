@@ -37,6 +37,20 @@ def oracle_threads(orc, n):
     orc.set_threads(min(16, orc.cpu_count()) if n >= 256 else 1)
 
 
+def oracle_iteration_range(orc, a, **kw) -> tuple[int, int]:
+    """The reference's own iteration count is not a single number at high
+    contrast: its OpenMP reductions change order with the thread count, and
+    where the residual plateaus near tol that moves the stopping iteration
+    (511^2 with a in {1e2, 1e-2}: 75 at 1-2 threads, 81 at 4+). Return the
+    range over one thread and all threads."""
+    counts = []
+    for t in (1, min(16, orc.cpu_count())):
+        orc.set_threads(t)
+        counts.append(orc.solve(a, **kw)["iterations"])
+    orc.set_threads(1)
+    return min(counts), max(counts)
+
+
 def true_residual(orc, a, u, f=1.0) -> float:
     """||b - A u|| / ||b|| on the CPU (b = f h^2)."""
     n = a.shape[0]
@@ -207,9 +221,10 @@ def test_grid_engine_matches_oracle(darcy, orc, n, cycle) -> None:
     oracle_threads(orc, n)
     want = orc.solve(a, tol=1e-10, cycle_index=cycle)
     orc.set_threads(1)
+    lo, hi = oracle_iteration_range(orc, a, tol=1e-10, cycle_index=cycle)
     got = darcy.solve(a, tol=1e-10, cycle_index=cycle)
     assert got.converged and got.levels == want["levels"]
-    assert abs(got.iterations - want["iterations"]) <= 1
+    assert lo - 1 <= got.iterations <= hi + 1, (got.iterations, lo, hi)
     assert rel_l2(got.u, want["u"]) < REL_L2
     assert got.residual < 1e-10
     # The recursive residual drifts from the true one at high contrast (the
