@@ -79,6 +79,30 @@ def lib() -> ctypes.CDLL:
         L.dgpu_flush_l2.argtypes = [_P, ctypes.c_int64]
         L.dgpu_apply_preconditioner_noalloc.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                                         ctypes.c_int, _P, _P]
+        # learned warm start
+        L.dgpu_net_create.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_P)]
+        L.dgpu_net_destroy.argtypes = [_P]
+        L.dgpu_net_destroy.restype = None
+        L.dgpu_net_num_params.argtypes = [_P]
+        L.dgpu_net_num_params.restype = ctypes.c_int64
+        L.dgpu_net_side.argtypes = [_P]
+        L.dgpu_net_get_params.argtypes = [_P, _P]
+        L.dgpu_net_set_params.argtypes = [_P, _P]
+        L.dgpu_net_get_scaling.argtypes = [_P, _P]
+        L.dgpu_net_set_scaling.argtypes = [_P, _P]
+        L.dgpu_net_set_engine.argtypes = [_P, ctypes.c_int]
+        L.dgpu_net_set_loss.argtypes = [_P, ctypes.c_int]
+        L.dgpu_net_load_pairs.argtypes = [_P, _P, _P, _P, ctypes.c_int64]
+        L.dgpu_net_train.argtypes = [_P, ctypes.c_int64, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong, _P]
+        L.dgpu_net_gradients.argtypes = [_P, _P, _P, _P, ctypes.c_int64, _P, _P]
+        L.dgpu_net_predict.argtypes = [_P, _P, _P, ctypes.c_int64, _P]
+        L.dgpu_net_features.argtypes = [_P, _P, _P, ctypes.c_int64, _P]
+        L.dgpu_net_predict_device.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _P]
+        L.dgpu_net_last_launches.argtypes = [_P]
+        L.dgpu_net_last_launches.restype = ctypes.c_int64
+        L.dgpu_net_info.argtypes = [_P, ctypes.c_char_p, ctypes.c_int]
+        L.dgpu_solve_batch_learned.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int64, ctypes.c_int64,
+                                               ctypes.POINTER(Options), _P, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -203,3 +227,130 @@ class Context:
 
     def flush_l2(self, nbytes: int = 512 << 20) -> None:
         check(lib().dgpu_flush_l2(self.handle, int(nbytes)))
+
+    def solve_batch_learned(self, net: "Net", a, f: float = 1.0, **kw) -> dict:
+        """solve_batch with the warm start predicted on the device by `net`."""
+        a = _f64(a)
+        batch, n = a.shape[0], a.shape[1]
+        u = np.empty_like(a)
+        it = np.zeros(batch, dtype=np.int32)
+        res = np.zeros(batch)
+        conv = np.zeros(batch, dtype=np.int32)
+        lev = np.zeros(batch, dtype=np.int32)
+        opt = options(**kw)
+        check(lib().dgpu_solve_batch_learned(self.handle, net.handle, _ptr(a), float(f), batch, n, ctypes.byref(opt),
+                                             _ptr(u), _ptr(it), _ptr(res), _ptr(conv), _ptr(lev)))
+        return {"u": u, "iterations": it, "residuals": res, "converged": conv.astype(bool), "levels": lev}
+
+
+ENGINE = {"tensor": 0, "simt": 1}
+LOSS = {"energy": 0, "mse": 1}
+
+
+class Net:
+    """Owns one dgpu_net (the warm-start network of include/darcy_gpu.h)."""
+
+    def __init__(self, side: int, seed: int = 0) -> None:
+        self.handle = _P()
+        check(lib().dgpu_net_create(int(side), int(seed) & ((1 << 64) - 1), ctypes.byref(self.handle)))
+        self.side = int(side)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().dgpu_net_destroy(self.handle)
+            self.handle = _P()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return int(lib().dgpu_net_num_params(self.handle))
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, dtype=np.float32)
+        check(lib().dgpu_net_get_params(self.handle, _ptr(out)))
+        return out
+
+    def set_params(self, w) -> None:
+        w = np.ascontiguousarray(np.asarray(w, dtype=np.float32))
+        if w.shape != (self.num_params,):
+            raise InvalidInput(f"expected {self.num_params} parameters, got shape {w.shape}")
+        check(lib().dgpu_net_set_params(self.handle, _ptr(w)))
+
+    def get_scaling(self) -> np.ndarray:
+        out = np.empty(4)
+        check(lib().dgpu_net_get_scaling(self.handle, _ptr(out)))
+        return out
+
+    def set_scaling(self, s) -> None:
+        s = _f64(s)
+        if s.shape != (4,):
+            raise InvalidInput("scaling has four entries: mean and std of log a, RMS of u, fref")
+        check(lib().dgpu_net_set_scaling(self.handle, _ptr(s)))
+
+    def set_engine(self, engine: str) -> None:
+        check(lib().dgpu_net_set_engine(self.handle, ENGINE[engine]))
+
+    def set_loss(self, kind: str) -> None:
+        check(lib().dgpu_net_set_loss(self.handle, LOSS[kind]))
+
+    def _pack(self, a, u=None, f=None):
+        a = _f64(a)
+        if a.ndim == 2:
+            a = a[None]
+        if a.ndim != 3 or a.shape[1] != self.side or a.shape[2] != self.side:
+            raise InvalidInput(f"a must have shape (count, {self.side}, {self.side})")
+        uu = None if u is None else _f64(u).reshape(a.shape)
+        ff = None
+        if f is not None and not np.isscalar(f):
+            ff = _f64(f).reshape(a.shape[0])
+        elif f is not None and float(f) != 1.0:
+            ff = np.full(a.shape[0], float(f))
+        return a, uu, ff
+
+    def load_pairs(self, a, u, f=None) -> None:
+        a, u, ff = self._pack(a, u, f)
+        check(lib().dgpu_net_load_pairs(self.handle, _ptr(a), _ptr(u), _ptr(ff), a.shape[0]))
+
+    def train(self, steps: int, batch: int = 256, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        losses = np.empty(int(steps), dtype=np.float32)
+        check(lib().dgpu_net_train(self.handle, int(steps), int(batch), float(lr), int(seed) & ((1 << 64) - 1),
+                                   _ptr(losses)))
+        return losses
+
+    def gradients(self, a, u, f=None) -> tuple[np.ndarray, float]:
+        a, u, ff = self._pack(a, u, f)
+        g = np.empty(self.num_params, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        check(lib().dgpu_net_gradients(self.handle, _ptr(a), _ptr(u), _ptr(ff), a.shape[0], _ptr(g), _ptr(loss)))
+        return g, float(loss[0])
+
+    def features(self, a, f=None) -> np.ndarray:
+        a, _, ff = self._pack(a, None, f)
+        out = np.empty(a.shape + (2,), dtype=np.float32)
+        check(lib().dgpu_net_features(self.handle, _ptr(a), _ptr(ff), a.shape[0], _ptr(out)))
+        return out
+
+    def predict(self, a, f=None) -> np.ndarray:
+        a, _, ff = self._pack(a, None, f)
+        u0 = np.empty_like(a)
+        check(lib().dgpu_net_predict(self.handle, _ptr(a), _ptr(ff), a.shape[0], _ptr(u0)))
+        return u0
+
+    def predict_device(self, d_a: int, count: int, d_u0: int, d_f: int | None = None,
+                       stream: int | None = None) -> None:
+        check(lib().dgpu_net_predict_device(self.handle, ctypes.c_void_p(d_a), ctypes.c_void_p(d_f) if d_f else None,
+                                            int(count), ctypes.c_void_p(d_u0),
+                                            ctypes.c_void_p(stream) if stream else None))
+
+    def info(self) -> str:
+        buf = ctypes.create_string_buffer(1024)
+        check(lib().dgpu_net_info(self.handle, buf, 1024))
+        return buf.value.decode()
+
+    def last_launches(self) -> int:
+        return int(lib().dgpu_net_last_launches(self.handle))

@@ -6,6 +6,10 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <string>
+
+#include "../../include/darcy_gpu.h"
+
 #include "common.cuh"
 #include "setup.cuh"
 
@@ -84,6 +88,12 @@ int num_levels_for(int n);
 
 // Message returned by dgpu_last_error() on this thread (solver.cu).
 void set_last_error(const char* msg);
+
+// Learned warm start (learn.cu), for the batched solve.
+int net_predict_on_stream(dgpu_net* net, const double* d_a, double fscalar, int64_t count, double* d_u0,
+                          cudaStream_t stream, std::string* msg);
+int net_side(const dgpu_net* net);
+int64_t net_launches(const dgpu_net* net);
 
 // Programmatic dependent launch for the grid engine's kernels (on by
 // default; DARCY_GPU_PDL=0 turns it off).

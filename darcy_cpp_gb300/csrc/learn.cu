@@ -1,0 +1,1634 @@
+// Learned warm start: a small convolutional network that predicts the initial
+// iterate u0 of PCG from (log a, f), trained on (a, u) pairs the GPU solver
+// produced. Every step runs in kernels written here (no library calls):
+//
+//   six 3x3 "same" convolutions, 2 -> 32 -> 32 -> 32 -> 32 -> 32 -> 1
+//   channels, GELU after the first five; BF16 activations and weights, FP32
+//   accumulation, FP32 master weights updated by Adam; loss = the error of
+//   the prediction in the energy norm of each sample's operator relative to
+//   the solution's (or plain mean squared error, on request).
+//
+// The four 32 -> 32 layers carry 97% of the arithmetic. They run as implicit
+// GEMMs on the 5th-generation tensor cores: a CTA takes a tile of 128
+// consecutive pixels (whole image rows when the side is <= 128), stages the
+// input rows it needs in shared memory as three column-shifted copies (dx =
+// -1, 0, +1, zero outside the image), and then every 16-wide K slice of the
+// 128 x 288 im2col matrix (tap (dy, dx), 16 channels) is a plain strided view
+// of one copy, so A needs no im2col pass: one tcgen05.mma (M 128, N 32,
+// K 16, BF16 in, FP32 accumulate in tensor memory) per slice, 18 per tile,
+// issued by one thread and completed through an mbarrier; tcgen05.ld brings
+// the accumulator back for the epilogue (bias + GELU, or the GELU derivative
+// in the backward pass). The input gradient of a 32 -> 32 layer is the same
+// kernel with the taps flipped and the channel roles of the weights swapped.
+// The 2 -> 32 and 32 -> 1 layers, the weight gradients (reductions over all
+// pixels, written per CTA and summed in a fixed order so training is
+// deterministic) and a CUDA-core version of the 32 -> 32 convolution (used
+// to check the tensor-core one) run on the CUDA cores.
+//
+// The reference has no learned component: this file extends its solve path
+// with the warm start x0 that PCG then refines to the same tolerance.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/darcy_gpu.h"
+#include "engine.h"
+
+namespace dgpu {
+namespace learn {
+
+constexpr int kC = 32;          // hidden channels
+constexpr int kLayers = 6;
+constexpr int kTaps = 9;
+constexpr int kK = kTaps * kC;  // 288: GEMM K of a 32 -> 32 layer
+constexpr int kTile = 128;      // GEMM M: positions per tile
+constexpr int kMaxSide = 512;
+
+typedef __nv_bfloat16 bf16;
+
+// Padded-position view of an H x W image: P = W + 2 columns per row (a zero
+// column either side), position s = r * P + c' holds pixel (r, c' - 1) for
+// 1 <= c' <= W. A tile is 128 consecutive positions; the positions a 3x3
+// stencil needs for it are the 128 + 2P + 2 starting P + 1 before the tile,
+// so every tap of every row of the tile is the same contiguous, uniformly
+// strided run of staged positions, shifted by dy * P + dx.
+struct Geom {
+    int H, W, P, tiles_per_img, nq;  // nq: staged positions per tile (multiple of 8)
+};
+
+inline bool side_supported(int s) { return s >= 8 && s <= kMaxSide && (s % 2) == 0; }
+
+inline Geom make_geom(int side) {
+    Geom g;
+    g.H = g.W = side;
+    g.P = side + 2;
+    g.tiles_per_img = (side * g.P + kTile - 1) / kTile;
+    g.nq = ((kTile + 2 * g.P + 2) + 7) & ~7;
+    return g;
+}
+
+// Tile t -> first pixel of its image and first padded position.
+__device__ __forceinline__ void tile_origin(int64_t t, const Geom& g, int64_t& pbase, int& s0) {
+    const int64_t b = t / g.tiles_per_img;
+    s0 = (int)(t - b * g.tiles_per_img) * kTile;
+    pbase = b * (int64_t)g.H * g.W;
+}
+
+// Pixel index (within the image) of padded position s, or -1 outside it.
+__device__ __forceinline__ int position_pixel(const Geom& g, int s) {
+    if (s < 0) return -1;
+    const int r = s / g.P, c = s - r * g.P;
+    if (r >= g.H || c < 1 || c > g.W) return -1;
+    return r * g.W + c - 1;
+}
+
+// ------------------------------------------------------------ elementwise
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+    return cdf + x * pdf;
+}
+
+template <class T>
+__device__ __forceinline__ float to_f(T v);
+template <>
+__device__ __forceinline__ float to_f<float>(float v) {
+    return v;
+}
+template <>
+__device__ __forceinline__ float to_f<bf16>(bf16 v) {
+    return __bfloat162float(v);
+}
+
+// ------------------------------------------------------ tcgen05 helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor, K-major, no swizzle: element (row, k) of
+// the operand is at start + (k / 8) * lbo + (row / 8) * sbo + (row % 8) * 16
+// + (k % 8) * 2.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t start, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((start >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // fixed field of the tcgen05 descriptor
+    return d;                // base offset 0, swizzle none
+}
+
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major.
+__host__ __device__ constexpr uint32_t mma_idesc(int M, int N) {
+    return (1u << 4)                       // D format: F32
+           | (1u << 7)                     // A format: BF16
+           | (1u << 10)                    // B format: BF16
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+// Bounded wait for an mbarrier phase: false if it did not complete within
+// `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, long long limit) {
+    for (long long i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+}
+
+// --------------------------------------------------------- featurisation
+
+// x0 = ((log a - mu) / sd, (f / fref) U1, 0 x 6) as 8 BF16 channels per pixel
+// (one 16-byte tensor-core chunk), U1 being the solution of the same grid for
+// a = 1 and f = 1 scaled to unit RMS: the forcing enters through the
+// constant-coefficient solution operator, which gives every pixel the global
+// shape of the solution that a 13 x 13 receptive field cannot see; target = u / (uscale
+// * f / fref) (the solution is linear in a constant f, so the network learns
+// the f = fref solution and the prediction is rescaled by f / fref).
+__global__ void k_featurize(const double* __restrict__ a, const double* __restrict__ u,
+                            const double* __restrict__ fs, int64_t count, int hw, double mu, double sd, double fref,
+                            double uscale, const float* __restrict__ u1, bf16* __restrict__ x0,
+                            float* __restrict__ target, float* __restrict__ af) {
+    const int64_t npix = count * hw;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        const double f = fs ? fs[p / hw] : 1.0;
+        __nv_bfloat162 v[4];
+        v[0] = __floats2bfloat162_rn((logf((float)a[p]) - (float)mu) / (float)sd, (float)(f / fref) * u1[p % hw]);
+        v[1] = v[2] = v[3] = __floats2bfloat162_rn(0.f, 0.f);
+        reinterpret_cast<uint4*>(x0)[p] = *reinterpret_cast<const uint4*>(v);
+        if (target) target[p] = (float)(u[p] / (uscale * f / fref));
+        if (af) af[p] = (float)a[p];
+    }
+}
+
+// ------------------------------------------------------ energy-norm loss
+//
+// The training loss is the error of the prediction in the energy norm of the
+// problem's own operator, e^T A e with e = out - target (A: harmonic face
+// coefficients, the permeability itself on the Dirichlet boundary faces,
+// level.hpp:79-97), relative to target^T A target, averaged over the batch.
+// This is the norm CG minimises, so it weights the error the way the solve
+// that starts from the prediction will see it (rough error costs far more
+// than smooth error of the same size).
+
+__device__ __forceinline__ float hface(float x, float y) { return 2.0f * x * y / (x + y); }
+
+// (A v)_p for image `img` (pixels pb .. pb + H W) at cell (i, j).
+__device__ __forceinline__ float apply_a(const float* __restrict__ v, const float* __restrict__ a, int64_t pb, int H,
+                                         int W, int i, int j) {
+    const int64_t p = pb + (int64_t)i * W + j;
+    const float ap = a[p], vp = v[p];
+    float y = 0.f;
+    y += (j + 1 < W) ? hface(ap, a[p + 1]) * (vp - v[p + 1]) : ap * vp;
+    y += (j > 0) ? hface(ap, a[p - 1]) * (vp - v[p - 1]) : ap * vp;
+    y += (i + 1 < H) ? hface(ap, a[p + W]) * (vp - v[p + W]) : ap * vp;
+    y += (i > 0) ? hface(ap, a[p - W]) * (vp - v[p - W]) : ap * vp;
+    return y;
+}
+
+constexpr int kEnergyThreads = 256;
+
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+// norm[s] = target_s^T A_s target_s, one CTA per sample.
+__global__ void __launch_bounds__(kEnergyThreads) k_sample_energy(const float* __restrict__ t,
+                                                                  const float* __restrict__ a, int H, int W,
+                                                                  float* __restrict__ norm) {
+    __shared__ double red[kEnergyThreads / 32];
+    const int64_t pb = (int64_t)blockIdx.x * H * W;
+    double s = 0.0;
+    for (int q = threadIdx.x; q < H * W; q += blockDim.x) {
+        const int i = q / W, j = q - (q / W) * W;
+        s += (double)t[pb + q] * (double)apply_a(t, a, pb, H, W, i, j);
+    }
+    const double tot = block_sum_d(s, red);
+    if (threadIdx.x == 0) norm[blockIdx.x] = (float)fmax(tot, 1e-30);
+}
+
+// Per sample: e = out - target, loss_s = e^T A e / norm_s and dout = 2 A e /
+// (batch norm_s), one CTA per sample.
+__global__ void __launch_bounds__(kEnergyThreads) k_energy_loss(const float* __restrict__ out,
+                                                                const float* __restrict__ target,
+                                                                const float* __restrict__ a,
+                                                                const float* __restrict__ norm, int H, int W,
+                                                                int batch, float* __restrict__ e,
+                                                                float* __restrict__ dout,
+                                                                float* __restrict__ part) {
+    __shared__ double red[kEnergyThreads / 32];
+    const int64_t pb = (int64_t)blockIdx.x * H * W;
+    for (int q = threadIdx.x; q < H * W; q += blockDim.x) e[pb + q] = out[pb + q] - target[pb + q];
+    __syncthreads();
+    const float sc = 2.0f / ((float)batch * norm[blockIdx.x]);
+    double s = 0.0;
+    for (int q = threadIdx.x; q < H * W; q += blockDim.x) {
+        const int i = q / W, j = q - (q / W) * W;
+        const float ae = apply_a(e, a, pb, H, W, i, j);
+        s += (double)e[pb + q] * (double)ae;
+        dout[pb + q] = sc * ae;
+    }
+    const double tot = block_sum_d(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = (float)(tot / (double)norm[blockIdx.x]);
+}
+
+// loss = mean of the per-sample parts, summed in order.
+__global__ void k_mean_parts(const float* __restrict__ part, int n, float* __restrict__ loss) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < n; ++q) s += part[q];
+        *loss = (float)(s / (double)n);
+    }
+}
+
+// u0 = out * uscale * f / fref in FP64.
+__global__ void k_unscale(const float* __restrict__ out, const double* __restrict__ fs, int64_t count, int hw,
+                          double uscale, double fref, double* __restrict__ u0) {
+    const int64_t npix = count * hw;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        const double f = fs ? fs[p / hw] : 1.0;
+        u0[p] = (double)out[p] * uscale * (f / fref);
+    }
+}
+
+// Per-block partial sums of log a, (log a)^2 and (u fref / f)^2 (fixed grid:
+// the host adds the partials in order, so the statistics are reproducible).
+constexpr int kStatBlocks = 256;
+__global__ void __launch_bounds__(256) k_stats(const double* __restrict__ a, const double* __restrict__ u,
+                                               const double* __restrict__ fs, int64_t count, int hw, double fref,
+                                               double* __restrict__ part) {
+    __shared__ double red[3][32];
+    double s1 = 0, s2 = 0, s3 = 0;
+    const int64_t npix = count * hw;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        const double la = log(a[p]);
+        s1 += la;
+        s2 += la * la;
+        const double f = fs ? fs[p / hw] : 1.0;
+        const double v = u[p] * fref / f;
+        s3 += v * v;
+    }
+    double s[3] = {s1, s2, s3};
+    for (int q = 0; q < 3; ++q) {
+        double v = s[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+        part[blockIdx.x * 3 + threadIdx.x] = v;
+    }
+}
+
+// Copies samples idx[0..batch) of the dataset into the batch buffers.
+__global__ void k_gather(const bf16* __restrict__ ds_x, const float* __restrict__ ds_t,
+                         const float* __restrict__ ds_a, const float* __restrict__ ds_norm,
+                         const int* __restrict__ idx, int batch, int hw, bf16* __restrict__ x0,
+                         float* __restrict__ target, float* __restrict__ af, float* __restrict__ norm) {
+    // per sample: x0 hw uint4 (8 BF16 channels a pixel), target and a hw / 4 uint4
+    const int per = hw + hw / 2;
+    const int64_t total = (int64_t)batch * per;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(q / per), r = (int)(q - (int64_t)s * per);
+        const int64_t src = idx[s];
+        if (r < hw) {
+            reinterpret_cast<uint4*>(x0)[(int64_t)s * hw + r] = reinterpret_cast<const uint4*>(ds_x)[src * hw + r];
+        } else if (r < hw + hw / 4) {
+            const int k = r - hw;
+            reinterpret_cast<uint4*>(target)[(int64_t)s * (hw / 4) + k] =
+                reinterpret_cast<const uint4*>(ds_t)[src * (hw / 4) + k];
+        } else {
+            const int k = r - hw - hw / 4;
+            reinterpret_cast<uint4*>(af)[(int64_t)s * (hw / 4) + k] =
+                reinterpret_cast<const uint4*>(ds_a)[src * (hw / 4) + k];
+        }
+        if (r == 0) norm[s] = ds_norm[src];
+    }
+}
+
+// ---------------------------------------------------- CUDA-core convolution
+//
+// y[p, co] = sum_{tap, ci} x[p + shift(tap), ci] w[co][tap * CIN + ci] with
+// zero padding, FP32 accumulation; one thread per (pixel, output channel); x
+// has XS >= CIN channels per pixel in memory.
+// Epilogue modes: 0 -> pre = y + bias (if pre), act = GELU(y + bias);
+// 1 -> act = y * GELU'(aux) (input gradient through the next GELU);
+// 2 -> outf = y + bias (the linear output layer).
+enum { kEpiGelu = 0, kEpiGeluGrad = 1, kEpiLinear = 2 };
+
+template <class TIN, int CIN, int XS = CIN>
+__global__ void k_conv_simt(const TIN* __restrict__ x, const bf16* __restrict__ wB, const float* __restrict__ bias,
+                            int cout, int H, int W, int64_t npix, int mode, const float* __restrict__ aux,
+                            float* __restrict__ pre, bf16* __restrict__ act, float* __restrict__ outf) {
+    const int64_t total = npix * cout;
+    const int hw = H * W;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int co = (int)(t % cout);
+        const int64_t p = t / cout;
+        const int64_t img = p / hw;
+        const int rem = (int)(p - img * hw);
+        const int i = rem / W, j = rem - (rem / W) * W;
+        float acc = 0.f;
+        const bf16* wr = wB + (int64_t)co * kTaps * CIN;
+        for (int tap = 0; tap < kTaps; ++tap) {
+            const int ii = i + tap / 3 - 1, jj = j + tap % 3 - 1;
+            if (ii < 0 || ii >= H || jj < 0 || jj >= W) continue;
+            const TIN* xr = x + ((img * H + ii) * W + jj) * XS;
+#pragma unroll 8
+            for (int ci = 0; ci < CIN; ++ci) acc += to_f(xr[ci]) * __bfloat162float(wr[tap * CIN + ci]);
+        }
+        if (mode == kEpiGelu) {
+            const float v = acc + bias[co];
+            if (pre) pre[t] = v;
+            act[t] = __float2bfloat16(gelu(v));
+        } else if (mode == kEpiGeluGrad) {
+            act[t] = __float2bfloat16(acc * gelu_grad(aux[t]));
+        } else {
+            outf[t] = acc + bias[co];
+        }
+    }
+}
+
+// ------------------------------------------------- tensor-core convolution
+//
+// One 3x3 layer as an implicit GEMM, 128 threads (4 warps) per CTA, one tile
+// of 128 padded positions at a time, the next tile's input staged (cp.async)
+// while the current one is multiplied and written back.
+//
+// Template: CCH = 16-byte input chunks per pixel (4: 32 channels; 1: the
+// 8-channel padded input of the first layer); NOUT = GEMM N (32 channels, or
+// 16 for the one-channel output layer, whose rows 1..15 are zero weights).
+//
+// Shared memory: B = the weights as K-major core matrices (16-byte chunk c of
+// row n at c * NOUT * 16 + n * 16), then two staging buffers; in a buffer,
+// chunk c of staged position q is at c * plane + q * 16 (plane = nq * 16).
+// K slices (16 wide) and their A views:
+//   CCH = 4: slice (tap, h) = channels 16h .. 16h + 15 of tap (dy, dx):
+//            start = 2h * plane + (dy P + dx) * 16, LBO = plane, SBO = 128;
+//   CCH = 1: slice j = taps 2j and 2j + 1 (tap 9 does not exist: its B
+//            chunk is zero and its A view repeats tap 8):
+//            start = shift(2j) * 16, LBO = (shift(2j + 1) - shift(2j)) * 16.
+// Epilogues: kEpiGelu (pre-activation FP32 if `pre`, GELU -> BF16 act),
+// kEpiGeluGrad (act = acc * GELU'(aux), BF16), kEpiLinear (outf = acc[0] + b).
+constexpr int kConvThreads = 128;
+constexpr long long kWaitLimit = 1ll << 24;  // mbarrier polls before a wait is declared lost
+
+template <int CCH, int NOUT>
+struct TcShape {
+    static constexpr int KCH = CCH == 4 ? 36 : 10;            // K chunks of B
+    static constexpr int SLICES = CCH == 4 ? 18 : 5;
+    static constexpr int B_BYTES = KCH * NOUT * 16;
+    static constexpr int K = KCH * 8;                         // bf16 per weight row
+};
+
+__host__ __device__ inline int tc_stage_bytes(int cch, int nq) { return cch * nq * 16; }
+
+template <int CCH, int NOUT>
+__host__ __device__ inline int tc_smem_bytes(int nq) {
+    return TcShape<CCH, NOUT>::B_BYTES + 2 * tc_stage_bytes(CCH, nq) + 128 + 16;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+template <int CCH>
+__device__ __forceinline__ void stage_tile(const bf16* __restrict__ x, const Geom& g, int64_t pbase, int s0,
+                                           uint32_t buf, uint32_t plane) {
+    for (int t = threadIdx.x; t < CCH * g.nq; t += kConvThreads) {
+        const int c = t / g.nq, q = t - c * g.nq;
+        const int pix = position_pixel(g, s0 - g.P - 1 + q);
+        const bf16* src = pix >= 0 ? x + ((pbase + pix) * CCH + c) * 8 : x;
+        cp_async16(buf + c * plane + q * 16, src, pix >= 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int CCH, int NOUT>
+__global__ void __launch_bounds__(kConvThreads) k_conv_tc(const bf16* __restrict__ x, const bf16* __restrict__ wB,
+                                                          const float* __restrict__ bias, Geom g, int64_t ntiles,
+                                                          int mode, const float* __restrict__ aux,
+                                                          float* __restrict__ pre, bf16* __restrict__ act,
+                                                          float* __restrict__ outf, int* __restrict__ err) {
+    using S = TcShape<CCH, NOUT>;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const uint32_t stage = tc_stage_bytes(CCH, g.nq);
+    unsigned char* sB = sm;
+    float* sBias = reinterpret_cast<float*>(sm + S::B_BYTES + 2 * stage);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + S::B_BYTES + 2 * stage + 128);
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t plane = g.nq * 16;
+
+    for (int q = tid; q < NOUT * S::KCH; q += kConvThreads) {
+        const int n = q / S::KCH, c = q - n * S::KCH;
+        *reinterpret_cast<uint4*>(sB + c * (NOUT * 16) + n * 16) =
+            *reinterpret_cast<const uint4*>(wB + (size_t)n * S::K + c * 8);
+    }
+    if (tid < 32) sBias[tid] = (bias && tid < NOUT) ? bias[tid] : 0.f;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(32u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init(smem_u32(mbar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    const uint32_t b_addr = smem_u32(sB), x_addr = smem_u32(sm + S::B_BYTES);
+    constexpr uint32_t idesc = mma_idesc(kTile, NOUT);
+    uint32_t phase = 0;
+    int buf = 0;
+
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles) {
+        int64_t pb;
+        int s0;
+        tile_origin(tile, g, pb, s0);
+        stage_tile<CCH>(x, g, pb, s0, x_addr, plane);
+    }
+    for (; tile < ntiles; tile += gridDim.x) {
+        int64_t pbase;
+        int s0;
+        tile_origin(tile, g, pbase, s0);
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        const uint32_t xb = x_addr + buf * stage;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+            for (int sl = 0; sl < S::SLICES; ++sl) {
+                uint32_t a_start, lbo;
+                if (CCH == 4) {
+                    const int tap = sl >> 1, h = sl & 1;
+                    const int dy = tap / 3, dx = tap - dy * 3;
+                    a_start = xb + (2 * h) * plane + (dy * g.P + dx) * 16;
+                    lbo = plane;
+                } else {
+                    const int t1 = 2 * sl, t2 = min(2 * sl + 1, 8);
+                    const int sh1 = (t1 / 3) * g.P + t1 % 3, sh2 = (t2 / 3) * g.P + t2 % 3;
+                    a_start = xb + sh1 * 16;
+                    lbo = (sh2 - sh1) * 16;
+                }
+                mma_bf16(tmem, smem_desc(a_start, lbo, 128),
+                         smem_desc(b_addr + sl * 2 * (NOUT * 16), NOUT * 16, 128), idesc, sl > 0 ? 1u : 0u);
+            }
+            mma_commit(smem_u32(mbar));
+        }
+        // stage the next tile into the other buffer while this one is multiplied
+        const int64_t next = tile + gridDim.x;
+        if (next < ntiles) {
+            int64_t pb;
+            int s1;
+            tile_origin(next, g, pb, s1);
+            stage_tile<CCH>(x, g, pb, s1, x_addr + (buf ^ 1) * stage, plane);
+        }
+        __syncwarp();
+        const bool ok = __syncthreads_and(mbar_wait(smem_u32(mbar), phase, kWaitLimit));
+        phase ^= 1u;
+        if (!ok) {
+            if (tid == 0) atomicExch(err, 1);
+            // give an MMA still in flight a bounded chance to land before the
+            // tensor memory is released
+            mbar_wait(smem_u32(mbar), phase ^ 1u, kWaitLimit);
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), v);
+        const int pix = position_pixel(g, s0 + tid);  // row tid of the tile
+        if (pix >= 0) {
+            const int64_t p = pbase + pix;
+            if (mode == kEpiLinear) {
+                outf[p] = v[0] + sBias[0];
+            } else {
+                if (mode == kEpiGelu) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) v[c] += sBias[c];
+                    if (pre) {
+                        float4* dst = reinterpret_cast<float4*>(pre + p * kC);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q)
+                            dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    }
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) v[c] = gelu(v[c]);
+                } else {  // kEpiGeluGrad
+                    const float4* src = reinterpret_cast<const float4*>(aux + p * kC);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float4 z = src[q];
+                        v[4 * q] *= gelu_grad(z.x);
+                        v[4 * q + 1] *= gelu_grad(z.y);
+                        v[4 * q + 2] *= gelu_grad(z.z);
+                        v[4 * q + 3] *= gelu_grad(z.w);
+                    }
+                }
+                uint4* dst = reinterpret_cast<uint4*>(act + p * kC);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t w[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const __nv_bfloat162 pr = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
+                        w[e] = *reinterpret_cast<const uint32_t*>(&pr);
+                    }
+                    dst[q] = make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();  // the accumulator and this buffer are reused two tiles on
+        buf ^= 1;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32u) : "memory");
+}
+
+// ------------------------------------------------------- weight gradients
+//
+// gW[co][tap * CIN + ci] = sum_p dy[p, co] x[p + shift(tap), ci] and gb[co] =
+// sum_p dy[p, co] over the CTA's tiles, written as one partial per CTA:
+// part[cta][co * (K + 1) + k] (k = K is the bias). With CIN = COUT = 32 a
+// thread owns one k and all 32 output channels; otherwise one (k, co) pair.
+template <int CIN, int COUT>
+struct Wgrad {
+    static constexpr int K = kTaps * CIN;
+    static constexpr int NV = (K + 1) * COUT;  // values per partial
+    static constexpr bool kAllCo = (CIN == 32 && COUT == 32);
+    static constexpr int kThreads = kAllCo ? ((K + 1 + 31) / 32) * 32 : ((NV + 31) / 32) * 32;
+};
+
+template <class TDY, int CIN, int XS, int COUT>
+__global__ void __launch_bounds__(Wgrad<CIN, COUT>::kThreads)
+    k_wgrad(const bf16* __restrict__ x, const TDY* __restrict__ dy, Geom g, int64_t ntiles, float* __restrict__ part) {
+    // x has XS channels per pixel in memory, of which the first CIN are used
+    using WG = Wgrad<CIN, COUT>;
+    constexpr int K = WG::K;
+    extern __shared__ __align__(16) unsigned char wsm[];
+    bf16* sX = reinterpret_cast<bf16*>(wsm);                                    // [nq][CIN]
+    float* sDy = reinterpret_cast<float*>(wsm + (((size_t)g.nq * CIN * 2 + 15) & ~(size_t)15));  // [128][COUT]
+    const int tid = threadIdx.x;
+
+    constexpr int CPT = WG::kAllCo ? COUT : 1;
+    float acc[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[c] = 0.f;
+    const int k = WG::kAllCo ? tid : tid / COUT;
+    const int co = WG::kAllCo ? 0 : tid - (tid / COUT) * COUT;
+    const bool active = WG::kAllCo ? (k <= K) : (tid < WG::NV);
+    int shift = 0, ci = 0;
+    if (active && k < K) {
+        const int tap = k / CIN;
+        ci = k - tap * CIN;
+        shift = (tap / 3) * g.P + tap % 3;
+    }
+
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        int64_t pbase;
+        int s0;
+        tile_origin(tile, g, pbase, s0);
+        for (int q = tid; q < g.nq * CIN; q += blockDim.x) {
+            const int pos = q / CIN, c = q - pos * CIN;
+            const int pix = position_pixel(g, s0 - g.P - 1 + pos);
+            sX[q] = pix >= 0 ? x[(pbase + pix) * XS + c] : __float2bfloat16(0.f);
+        }
+        for (int q = tid; q < kTile * COUT; q += blockDim.x) {
+            const int m = q / COUT, c = q - m * COUT;
+            const int pix = position_pixel(g, s0 + m);
+            sDy[q] = pix >= 0 ? to_f(dy[(pbase + pix) * COUT + c]) : 0.f;
+        }
+        __syncthreads();
+        if (active) {
+            for (int m = 0; m < kTile; ++m) {
+                const float xv = (k < K) ? __bfloat162float(sX[(m + shift) * CIN + ci]) : 1.0f;
+                if (WG::kAllCo) {
+#pragma unroll
+                    for (int q = 0; q < COUT / 4; ++q) {
+                        const float4 d = *reinterpret_cast<const float4*>(&sDy[m * COUT + 4 * q]);
+                        acc[4 * q] += d.x * xv;
+                        acc[4 * q + 1] += d.y * xv;
+                        acc[4 * q + 2] += d.z * xv;
+                        acc[4 * q + 3] += d.w * xv;
+                    }
+                } else {
+                    acc[0] += sDy[m * COUT + co] * xv;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (active) {
+        float* out = part + (int64_t)blockIdx.x * WG::NV;
+        if (WG::kAllCo) {
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) out[c * (K + 1) + k] = acc[c];
+        } else {
+            out[co * (K + 1) + k] = acc[0];
+        }
+    }
+}
+
+inline size_t wgrad_smem(const Geom& g, int cin, int cout) {
+    return (((size_t)g.nq * cin * 2 + 15) & ~(size_t)15) + (size_t)kTile * cout * 4;
+}
+
+// Sums the per-CTA partials in CTA order into the layer's weight and bias
+// gradients (master layout: w[co][k], then b[co]).
+__global__ void k_reduce_wgrad(const float* __restrict__ part, int nparts, int nv, int K, float* __restrict__ gw,
+                               float* __restrict__ gb) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nv; j += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int q = 0; q < nparts; ++q) s += part[(int64_t)q * nv + j];
+        const int co = j / (K + 1), k = j - co * (K + 1);
+        if (k < K)
+            gw[co * K + k] = s;
+        else
+            gb[co] = s;
+    }
+}
+
+// ---------------------------------------------------------------- loss
+
+constexpr int kLossBlocks = 256, kLossThreads = 256;
+
+// dout = 2 (out - target) / npix; per-block partial sums of (out - target)^2.
+__global__ void __launch_bounds__(kLossThreads) k_mse(const float* __restrict__ out, const float* __restrict__ target,
+                                                      int64_t npix, float* __restrict__ dout,
+                                                      float* __restrict__ part) {
+    __shared__ float red[kLossThreads / 32];
+    float s = 0.f;
+    const float sc = 2.0f / (float)npix;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        const float d = out[p] - target[p];
+        s += d * d;
+        dout[p] = sc * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < kLossThreads / 32; ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_mse_final(const float* __restrict__ part, int nparts, int64_t npix, float* __restrict__ loss) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < nparts; ++q) s += part[q];
+        *loss = (float)(s / (double)npix);
+    }
+}
+
+// ---------------------------------------------------------------- Adam
+
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, int n, float lr, float b1, float b2, float eps, float bc1, float bc2) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const float gj = g[j];
+        const float a = b1 * m1[j] + (1.f - b1) * gj;
+        const float b = b2 * m2[j] + (1.f - b2) * gj * gj;
+        m1[j] = a;
+        m2[j] = b;
+        w[j] -= lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+    }
+}
+
+struct LayerTable {
+    int off_w[kLayers], off_b[kLayers], cin[kLayers], cout[kLayers];
+    int64_t off_f[kLayers], off_t[kLayers];  // bf16 forward [cout][K] and flipped [cin][9 cout] forms
+    int64_t off_tc0, off_tc5;  // tensor-core forms of the first ([32][80]) and last ([16][288]) layers
+};
+
+// BF16 copies of the weights: forward form wf[co][tap * cin + ci], the
+// input-gradient form wt[ci][(8 - tap) * cout + co] (the transposed
+// convolution is a convolution with the taps flipped), and the zero-padded
+// tensor-core forms of the first layer (8 input channels a tap, a tenth zero
+// chunk) and the last (16 output rows). Padding entries are zero from creation.
+__global__ void k_cast_weights(const float* __restrict__ w, LayerTable T, bf16* __restrict__ wb) {
+    for (int l = 0; l < kLayers; ++l) {
+        const int cin = T.cin[l], cout = T.cout[l], K = kTaps * cin, nw = cout * K;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nw; j += gridDim.x * blockDim.x) {
+            const bf16 v = __float2bfloat16(w[T.off_w[l] + j]);
+            const int co = j / K, k = j - co * K;
+            const int tap = k / cin, ci = k - tap * cin;
+            wb[T.off_f[l] + j] = v;
+            wb[T.off_t[l] + (int64_t)ci * kTaps * cout + (8 - tap) * cout + co] = v;
+            if (l == 0) wb[T.off_tc0 + (int64_t)co * 80 + tap * 8 + ci] = v;
+            if (l == kLayers - 1) wb[T.off_tc5 + k] = v;  // row 0 of [16][288]
+        }
+    }
+}
+
+}  // namespace learn
+}  // namespace dgpu
+
+// ===================================================================== host
+
+using namespace dgpu;
+using namespace dgpu::learn;
+
+namespace {
+
+struct NetFailure {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void net_invalid(const std::string& m) { throw NetFailure{DGPU_INVALID_INPUT, m}; }
+
+#define NCK(call)                                                                                        \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            throw NetFailure{DGPU_CUDA_ERROR, std::string("CUDA error ") + cudaGetErrorName(e_) + " (" +     \
+                                                  cudaGetErrorString(e_) + ") in " #call};               \
+    } while (0)
+
+template <class T>
+struct Buf {
+    T* p = nullptr;
+    size_t n = 0;
+    Buf() = default;
+    Buf(const Buf&) = delete;
+    Buf& operator=(const Buf&) = delete;
+    ~Buf() {
+        if (p) cudaFree(p);
+    }
+    T* ensure(size_t count) {
+        if (count <= n && p) return p;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        NCK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        n = std::max<size_t>(count, 1);
+        return p;
+    }
+};
+
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double uniform01(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+int grid_for(int64_t work, int threads, int sms) {
+    const int64_t b = (work + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sms * 8));
+}
+
+}  // namespace
+
+struct dgpu_net {
+    std::mutex mu;
+    int device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    Geom g{};
+    int hw = 0;
+    int engine = DGPU_NET_TENSOR;
+    LayerTable T{};
+    int nparams = 0;
+    int64_t nwb = 0;
+    Buf<float> w, grad, m1, m2, gpart, loss_part, losses;
+    Buf<bf16> wb;
+    Buf<int> err, idx;
+    // batch buffers
+    int64_t cap = 0, cap_train = 0;  // samples the batch buffers hold
+    Buf<bf16> x0, act[5], dpre[2];
+    Buf<float> pre[5], out, target, dout, af, err_e, norm;
+    // dataset
+    int64_t ds_count = 0;
+    Buf<bf16> ds_x;
+    Buf<float> ds_t, ds_a, ds_norm;
+    int loss_kind = DGPU_NET_LOSS_ENERGY;
+    Buf<double> stage_a, stage_u, stage_f, stage_u0;
+    Buf<double> stat_part;
+    Buf<float> u1;  // unit-RMS solution for a = 1, f = 1 (feature channel 1)
+    // scaling
+    bool have_scaling = false;
+    double mu_la = 0.0, sd_la = 1.0, uscale = 1.0, fref = 1.0;
+    int64_t step = 0;
+    int ctas_tc32 = 0, ctas_tc_in = 0, ctas_tc_out = 0;  // persistent grid of each tensor-core instance
+    int wg_ctas = 0;
+    int64_t launches = 0;  // kernels launched by the last call
+    std::string info;      // launch shapes chosen at creation
+    ~dgpu_net() {
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int net_run(const std::function<void()>& fn) {
+    try {
+        fn();
+        set_last_error("");
+        return DGPU_OK;
+    } catch (const NetFailure& e) {
+        set_last_error(e.msg.c_str());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("out of host memory");
+        return DGPU_NO_MEMORY;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return DGPU_CUDA_ERROR;
+    }
+}
+
+// Batch buffers for `count` samples: activations always, pre-activations and
+// gradients only for training.
+void ensure_batch(dgpu_net* N, int64_t count, bool train) {
+    const size_t np = (size_t)count * N->hw;
+    if (count > N->cap) {
+        N->x0.ensure(np * 8);
+        for (int l = 0; l < 5; ++l) N->act[l].ensure(np * kC);
+        N->out.ensure(np);
+        N->cap = count;
+    }
+    if (train && count > N->cap_train) {
+        for (int l = 0; l < 5; ++l) N->pre[l].ensure(np * kC);
+        N->dpre[0].ensure(np * kC);
+        N->dpre[1].ensure(np * kC);
+        N->target.ensure(np);
+        N->dout.ensure(np);
+        N->af.ensure(np);
+        N->err_e.ensure(np);
+        N->norm.ensure(count);
+        N->loss_part.ensure(std::max<int64_t>(count, kLossBlocks));
+        N->cap_train = count;
+    }
+}
+
+void launched(dgpu_net* N, int k = 1) {
+    NCK(cudaGetLastError());
+    N->launches += k;
+}
+
+void cast_weights(dgpu_net* N) {
+    k_cast_weights<<<grid_for(kC * kK, 256, N->sms), 256, 0, N->stream>>>(N->w.p, N->T, N->wb.p);
+    launched(N);
+}
+
+const bf16* wf(dgpu_net* N, int l) { return N->wb.p + N->T.off_f[l]; }
+const bf16* wt(dgpu_net* N, int l) { return N->wb.p + N->T.off_t[l]; }
+const float* bias_of(dgpu_net* N, int l) { return N->w.p + N->T.off_b[l]; }
+
+template <int CCH, int NOUT>
+void launch_tc(dgpu_net* N, int ctas_cap, const bf16* x, const bf16* wB, const float* b, int64_t count, int mode,
+               const float* aux, float* pre, bf16* act, float* outf) {
+    const int64_t ntiles = count * N->g.tiles_per_img;
+    const int ctas = (int)std::min<int64_t>(ntiles, ctas_cap);
+    k_conv_tc<CCH, NOUT><<<ctas, kConvThreads, tc_smem_bytes<CCH, NOUT>(N->g.nq), N->stream>>>(
+        x, wB, b, N->g, ntiles, mode, aux, pre, act, outf, N->err.p);
+    launched(N);
+}
+
+// One 32 -> 32 convolution on the selected engine.
+void conv32(dgpu_net* N, const bf16* x, const bf16* wB, const float* b, int64_t count, int mode, const float* aux,
+            float* pre, bf16* act) {
+    const int64_t npix = count * N->hw;
+    if (N->engine == DGPU_NET_TENSOR) {
+        launch_tc<4, 32>(N, N->ctas_tc32, x, wB, b, count, mode, aux, pre, act, nullptr);
+    } else {
+        k_conv_simt<bf16, 32><<<grid_for(npix * kC, 256, N->sms), 256, 0, N->stream>>>(
+            x, wB, b, kC, N->g.H, N->g.W, npix, mode, aux, pre, act, nullptr);
+        launched(N);
+    }
+}
+
+// Forward pass over `count` samples already in x0. With keep = false the
+// pre-activations are not stored (prediction only).
+void forward(dgpu_net* N, int64_t count, bool keep) {
+    const int64_t npix = count * N->hw;
+    if (N->engine == DGPU_NET_TENSOR)
+        launch_tc<1, 32>(N, N->ctas_tc_in, N->x0.p, N->wb.p + N->T.off_tc0, bias_of(N, 0), count, kEpiGelu, nullptr,
+                         keep ? N->pre[0].p : nullptr, N->act[0].p, nullptr);
+    else {
+        k_conv_simt<bf16, 2, 8><<<grid_for(npix * kC, 256, N->sms), 256, 0, N->stream>>>(
+            N->x0.p, wf(N, 0), bias_of(N, 0), kC, N->g.H, N->g.W, npix, kEpiGelu, nullptr,
+            keep ? N->pre[0].p : nullptr, N->act[0].p, nullptr);
+        launched(N);
+    }
+    for (int l = 1; l <= 4; ++l)
+        conv32(N, N->act[l - 1].p, wf(N, l), bias_of(N, l), count, kEpiGelu, nullptr, keep ? N->pre[l].p : nullptr,
+               N->act[l].p);
+    if (N->engine == DGPU_NET_TENSOR)
+        launch_tc<4, 16>(N, N->ctas_tc_out, N->act[4].p, N->wb.p + N->T.off_tc5, bias_of(N, 5), count, kEpiLinear,
+                         nullptr, nullptr, nullptr, N->out.p);
+    else {
+        k_conv_simt<bf16, 32><<<grid_for(npix, 256, N->sms), 256, 0, N->stream>>>(
+            N->act[4].p, wf(N, 5), bias_of(N, 5), 1, N->g.H, N->g.W, npix, kEpiLinear, nullptr, nullptr, nullptr,
+            N->out.p);
+        launched(N);
+    }
+}
+
+template <class TDY, int CIN, int XS, int COUT>
+void wgrad(dgpu_net* N, const bf16* x, const TDY* dy, int64_t count, int layer) {
+    using WG = Wgrad<CIN, COUT>;
+    const int64_t ntiles = count * N->g.tiles_per_img;
+    const int ctas = (int)std::min<int64_t>(ntiles, N->wg_ctas);
+    k_wgrad<TDY, CIN, XS, COUT><<<ctas, WG::kThreads, wgrad_smem(N->g, CIN, COUT), N->stream>>>(x, dy, N->g, ntiles,
+                                                                                              N->gpart.p);
+    launched(N);
+    k_reduce_wgrad<<<grid_for(WG::NV, 256, N->sms), 256, 0, N->stream>>>(
+        N->gpart.p, ctas, WG::NV, WG::K, N->grad.p + N->T.off_w[layer], N->grad.p + N->T.off_b[layer]);
+    launched(N);
+}
+
+// Loss, then the gradient of every parameter into N->grad (batch in x0 / target).
+void backward(dgpu_net* N, int64_t count, float* loss_slot) {
+    const int64_t npix = count * N->hw;
+    if (N->loss_kind == DGPU_NET_LOSS_ENERGY) {
+        k_energy_loss<<<(int)count, kEnergyThreads, 0, N->stream>>>(N->out.p, N->target.p, N->af.p, N->norm.p,
+                                                                    N->g.H, N->g.W, (int)count, N->err_e.p,
+                                                                    N->dout.p, N->loss_part.p);
+        launched(N);
+        k_mean_parts<<<1, 32, 0, N->stream>>>(N->loss_part.p, (int)count, loss_slot);
+        launched(N);
+    } else {
+        k_mse<<<kLossBlocks, kLossThreads, 0, N->stream>>>(N->out.p, N->target.p, npix, N->dout.p,
+                                                            N->loss_part.p);
+        launched(N);
+        k_mse_final<<<1, 32, 0, N->stream>>>(N->loss_part.p, kLossBlocks, npix, loss_slot);
+        launched(N);
+    }
+    // output layer (32 -> 1): weight gradient, then the input gradient through
+    // the GELU of layer 4 (a 1 -> 32 convolution with the flipped weights)
+    wgrad<float, 32, 32, 1>(N, N->act[4].p, N->dout.p, count, 5);
+    k_conv_simt<float, 1><<<grid_for(npix * kC, 256, N->sms), 256, 0, N->stream>>>(
+        N->dout.p, wt(N, 5), nullptr, kC, N->g.H, N->g.W, npix, kEpiGeluGrad, N->pre[4].p, nullptr, N->dpre[0].p,
+        nullptr);
+    launched(N);
+    int cur = 0;  // dpre[cur] holds the gradient at layer l's pre-activation
+    for (int l = 4; l >= 1; --l) {
+        wgrad<bf16, 32, 32, 32>(N, N->act[l - 1].p, N->dpre[cur].p, count, l);
+        conv32(N, N->dpre[cur].p, wt(N, l), nullptr, count, kEpiGeluGrad, N->pre[l - 1].p, nullptr,
+               N->dpre[cur ^ 1].p);
+        cur ^= 1;
+    }
+    wgrad<bf16, 2, 8, 32>(N, N->x0.p, N->dpre[cur].p, count, 0);
+}
+
+void adam_step(dgpu_net* N, float lr) {
+    N->step += 1;
+    const double b1 = 0.9, b2 = 0.999;
+    const float bc1 = (float)(1.0 - std::pow(b1, (double)N->step));
+    const float bc2 = (float)(1.0 - std::pow(b2, (double)N->step));
+    k_adam<<<grid_for(N->nparams, 256, N->sms), 256, 0, N->stream>>>(N->w.p, N->grad.p, N->m1.p, N->m2.p, N->nparams,
+                                                                      lr, (float)b1, (float)b2, 1e-8f, bc1, bc2);
+    launched(N);
+    cast_weights(N);
+}
+
+void check_err(dgpu_net* N) {
+    int e = 0;
+    NCK(cudaMemcpyAsync(&e, N->err.p, sizeof(int), cudaMemcpyDeviceToHost, N->stream));
+    NCK(cudaStreamSynchronize(N->stream));
+    if (e) {
+        NCK(cudaMemsetAsync(N->err.p, 0, sizeof(int), N->stream));
+        throw NetFailure{DGPU_TIMEOUT, "tensor-core convolution: an MMA completion wait ran out"};
+    }
+}
+
+// Featurises `count` samples (host or device arrays) into x0 / target.
+// Host f values are staged into stage_f.
+void featurize_into(dgpu_net* N, const double* a, const double* u, const double* f, int64_t count, bool device,
+                    bf16* x0, float* target, float* af = nullptr, float* norm = nullptr) {
+    const size_t np = (size_t)count * N->hw;
+    const double* da = a;
+    const double* du = u;
+    const double* df = f;
+    if (!device) {
+        double* sa = N->stage_a.ensure(np);
+        NCK(cudaMemcpyAsync(sa, a, np * sizeof(double), cudaMemcpyHostToDevice, N->stream));
+        da = sa;
+        if (u) {
+            double* su = N->stage_u.ensure(np);
+            NCK(cudaMemcpyAsync(su, u, np * sizeof(double), cudaMemcpyHostToDevice, N->stream));
+            du = su;
+        }
+        if (f) {
+            double* sf = N->stage_f.ensure(count);
+            NCK(cudaMemcpyAsync(sf, f, count * sizeof(double), cudaMemcpyHostToDevice, N->stream));
+            df = sf;
+        }
+    }
+    k_featurize<<<grid_for((int64_t)np, 256, N->sms), 256, 0, N->stream>>>(
+        da, du, df, count, N->hw, N->mu_la, N->sd_la, N->fref, N->uscale, N->u1.p, x0, target, af);
+    launched(N);
+    if (norm) {
+        k_sample_energy<<<(int)count, kEnergyThreads, 0, N->stream>>>(target, af, N->g.H, N->g.W, norm);
+        launched(N);
+    }
+}
+
+void check_net(const dgpu_net* N) {
+    if (!N) net_invalid("network must not be NULL");
+}
+
+void check_samples(const double* a, int64_t count) {
+    if (count < 1) net_invalid("need at least one sample");
+    if (!a) net_invalid("buffers must not be NULL");
+}
+
+// The reference's permeability check (solver.hpp:68-77) on host samples.
+void check_a_host(const double* a, int64_t cells) {
+    for (int64_t k = 0; k < cells; ++k)
+        if (!(a[k] > 0.0) || !std::isfinite(a[k]))
+            net_invalid("permeability must be finite and strictly positive everywhere; offending value at flat index " +
+                        std::to_string(k));
+}
+
+void check_f_host(const double* f, int64_t count) {
+    if (!f) return;
+    for (int64_t q = 0; q < count; ++q)
+        if (!(f[q] != 0.0) || !std::isfinite(f[q])) net_invalid("f must be finite and non-zero per sample");
+}
+
+void predict_impl(dgpu_net* net, const double* a, const double* f, int64_t count, double* u0, bool device,
+                  cudaStream_t user) {
+    if (!net->have_scaling) net_invalid("scaling not set: train or load the network first");
+    const int64_t chunk = std::min<int64_t>(count, std::max<int64_t>(1, (int64_t)(4 << 20) / net->hw));
+    ensure_batch(net, chunk, false);
+    net->launches = 0;
+    if (device && user) {  // order after the caller's stream
+        cudaEvent_t ev;
+        NCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        NCK(cudaEventRecord(ev, user));
+        NCK(cudaStreamWaitEvent(net->stream, ev, 0));
+        NCK(cudaEventDestroy(ev));
+    }
+    for (int64_t at = 0; at < count; at += chunk) {
+        const int64_t c = std::min(chunk, count - at);
+        const size_t np = (size_t)c * net->hw;
+        featurize_into(net, a + at * net->hw, nullptr, f ? f + at : nullptr, c, device, net->x0.p, nullptr);
+        forward(net, c, false);
+        const double* dfs = f ? (device ? f + at : net->stage_f.p) : nullptr;
+        double* dst = u0 + at * net->hw;
+        double* tmp = device ? dst : net->stage_u0.ensure(np);
+        k_unscale<<<grid_for((int64_t)np, 256, net->sms), 256, 0, net->stream>>>(net->out.p, dfs, c, net->hw,
+                                                                                 net->uscale, net->fref, tmp);
+        launched(net);
+        if (!device) {
+            NCK(cudaMemcpyAsync(dst, tmp, np * sizeof(double), cudaMemcpyDeviceToHost, net->stream));
+            NCK(cudaStreamSynchronize(net->stream));  // staging reused by the next chunk
+        }
+    }
+    if (device && user) {
+        cudaEvent_t ev;
+        NCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        NCK(cudaEventRecord(ev, net->stream));
+        NCK(cudaStreamWaitEvent(user, ev, 0));
+        NCK(cudaEventDestroy(ev));
+    }
+    if (!device) check_err(net);
+}
+
+}  // namespace
+
+// Solution of the n x n grid for a = 1, f = 1 (the 5-point Dirichlet
+// Laplacian T (x) I + I (x) T, T = tridiag(-1, 2, -1), right-hand side h^2,
+// h = 1 / (n + 1)), from its sine eigenvectors v_k(i) = sqrt(2 / (n + 1))
+// sin(pi k (i + 1) / (n + 1)) and eigenvalues mu_k = 2 - 2 cos(pi k / (n + 1)):
+// U = h^2 sum_kl c_k c_l v_k v_l^T / (mu_k + mu_l), c_k = sum_i v_k(i).
+// Returned scaled to unit RMS.
+std::vector<double> unit_solution(int n) {
+    const double pi = 3.14159265358979323846, h = 1.0 / (n + 1);
+    std::vector<double> v((size_t)n * n), mu(n), c(n, 0.0);
+    for (int k = 0; k < n; ++k) {
+        mu[k] = 2.0 - 2.0 * std::cos(pi * (k + 1) / (n + 1));
+        for (int i = 0; i < n; ++i) {
+            v[(size_t)k * n + i] = std::sqrt(2.0 / (n + 1)) * std::sin(pi * (k + 1) * (i + 1) / (n + 1));
+            c[k] += v[(size_t)k * n + i];
+        }
+    }
+    std::vector<double> M((size_t)n * n, 0.0), U((size_t)n * n, 0.0);
+    for (int k = 0; k < n; ++k)
+        for (int l = 0; l < n; ++l) {
+            const double w = c[l] / (mu[k] + mu[l]);
+            if (w == 0.0) continue;
+            for (int j = 0; j < n; ++j) M[(size_t)k * n + j] += w * v[(size_t)l * n + j];
+        }
+    for (int k = 0; k < n; ++k) {
+        const double ck = h * h * c[k];
+        if (ck == 0.0) continue;
+        for (int i = 0; i < n; ++i) {
+            const double a = ck * v[(size_t)k * n + i];
+            for (int j = 0; j < n; ++j) U[(size_t)i * n + j] += a * M[(size_t)k * n + j];
+        }
+    }
+    double ss = 0.0;
+    for (double x : U) ss += x * x;
+    const double rms = std::sqrt(ss / ((double)n * n));
+    for (double& x : U) x /= rms;
+    return U;
+}
+
+// Persistent grid of one tensor-core instance: resident CTAs per SM (shared
+// memory and tensor-memory columns allow) times the SM count.
+template <int CCH, int NOUT>
+int tc_grid(dgpu_net* N, std::string* info) {
+    const int smem = tc_smem_bytes<CCH, NOUT>(N->g.nq);
+    NCK(cudaFuncSetAttribute(k_conv_tc<CCH, NOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    NCK(cudaFuncSetAttribute(k_conv_tc<CCH, NOUT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int api = 0;
+    NCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&api, k_conv_tc<CCH, NOUT>, kConvThreads, smem));
+    // the same bound from the resources themselves: shared memory, registers, threads
+    cudaFuncAttributes fa{};
+    NCK(cudaFuncGetAttributes(&fa, k_conv_tc<CCH, NOUT>));
+    int smem_sm = 0, regs_sm = 0, thr_sm = 0, reserved = 0;
+    NCK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, N->device));
+    NCK(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, N->device));
+    NCK(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, N->device));
+    NCK(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, N->device));
+    const int by_smem = smem_sm / (smem + (int)fa.sharedSizeBytes + reserved);
+    const int by_regs = regs_sm / std::max(1, fa.numRegs * kConvThreads);
+    const int by_thr = thr_sm / kConvThreads;
+    const int manual = std::min(std::min(by_smem, by_regs), std::min(by_thr, 16));  // 16 x 32 TMEM columns
+    const int per_sm = std::max(1, std::max(api, manual));
+    char buf[200];
+    std::snprintf(buf, sizeof buf, "tc<%d,%d>: smem %d B, %d regs, occupancy api %d / resources %d -> %d CTAs/SM; ",
+                  CCH, NOUT, smem + (int)fa.sharedSizeBytes, fa.numRegs, api, manual, per_sm);
+    *info += buf;
+    return N->sms * per_sm;
+}
+
+template <class TDY, int CIN, int XS, int COUT>
+void set_wgrad_smem(const Geom& g) {
+    NCK(cudaFuncSetAttribute(k_wgrad<TDY, CIN, XS, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)wgrad_smem(g, CIN, COUT)));
+}
+
+namespace dgpu {
+// Used by the batched solve with a learned warm start (solver.cu): predicts
+// u0 for `count` problems of the network's side whose permeability is already
+// on the device, ordered on `stream`. Returns a DGPU_* status and its message.
+int net_predict_on_stream(dgpu_net* net, const double* d_a, double fscalar, int64_t count, double* d_u0,
+                          cudaStream_t stream, std::string* msg) {
+    std::lock_guard<std::mutex> lock(net->mu);
+    try {
+        NCK(cudaSetDevice(net->device));
+        if (fscalar == 0.0 || !std::isfinite(fscalar)) net_invalid("f must be finite and non-zero for the warm start");
+        double* df = nullptr;
+        if (fscalar != 1.0) {
+            df = net->stage_f.ensure(count);
+            std::vector<double> h((size_t)count, fscalar);
+            NCK(cudaMemcpyAsync(df, h.data(), sizeof(double) * count, cudaMemcpyHostToDevice, net->stream));
+            NCK(cudaStreamSynchronize(net->stream));
+        }
+        predict_impl(net, d_a, df, count, d_u0, true, stream);
+        return DGPU_OK;
+    } catch (const NetFailure& e) {
+        *msg = e.msg;
+        return e.code;
+    }
+}
+int net_side(const dgpu_net* net) { return net ? net->g.W : 0; }
+int64_t net_launches(const dgpu_net* net) { return net ? net->launches : 0; }
+bool net_error_pending(dgpu_net* net) {
+    int e = 0;
+    cudaMemcpyAsync(&e, net->err.p, sizeof(int), cudaMemcpyDeviceToHost, net->stream);
+    cudaStreamSynchronize(net->stream);
+    if (e) cudaMemsetAsync(net->err.p, 0, sizeof(int), net->stream);
+    return e != 0;
+}
+}  // namespace dgpu
+
+extern "C" {
+
+int dgpu_net_create(int side, unsigned long long seed, dgpu_net** out) {
+    return net_run([&] {
+        if (!out) net_invalid("output pointer must not be NULL");
+        *out = nullptr;
+        if (!side_supported(side))
+            net_invalid("network side must be even and in 8..512 (got " + std::to_string(side) + ")");
+        std::unique_ptr<dgpu_net> N(new dgpu_net);
+        NCK(cudaGetDevice(&N->device));
+        NCK(cudaDeviceGetAttribute(&N->sms, cudaDevAttrMultiProcessorCount, N->device));
+        int major = 0, minor = 0;
+        NCK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, N->device));
+        NCK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, N->device));
+        if (major * 10 + minor != 103)
+            throw NetFailure{DGPU_CUDA_ERROR, "the warm-start network's kernels are built for sm_103a (GB300)"};
+        NCK(cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking));
+        N->g = make_geom(side);
+        N->hw = side * side;
+        const int cin[kLayers] = {2, kC, kC, kC, kC, kC};
+        const int cout[kLayers] = {kC, kC, kC, kC, kC, 1};
+        int off = 0;
+        int64_t offb = 0;
+        for (int l = 0; l < kLayers; ++l) {
+            N->T.cin[l] = cin[l];
+            N->T.cout[l] = cout[l];
+            N->T.off_w[l] = off;
+            off += cout[l] * kTaps * cin[l];
+            N->T.off_b[l] = off;
+            off += cout[l];
+            N->T.off_f[l] = offb;
+            offb += (int64_t)cout[l] * kTaps * cin[l];
+            offb = (offb + 7) & ~(int64_t)7;  // 16-byte aligned rows for the tensor-core loads
+            N->T.off_t[l] = offb;
+            offb += (int64_t)cout[l] * kTaps * cin[l];
+            offb = (offb + 7) & ~(int64_t)7;
+        }
+        N->T.off_tc0 = offb;
+        offb += 32 * 80;
+        N->T.off_tc5 = offb;
+        offb += 16 * kK;
+        N->nparams = off;
+        N->nwb = offb;
+        // He-uniform initialisation (the output layer scaled down), biases 0
+        std::vector<float> h(off, 0.f);
+        uint64_t s = seed ^ 0xD1B54A32D192ED03ull;
+        for (int l = 0; l < kLayers; ++l) {
+            const double lim = std::sqrt(6.0 / (kTaps * cin[l])) * (l == kLayers - 1 ? 0.1 : 1.0);
+            for (int j = 0; j < cout[l] * kTaps * cin[l]; ++j)
+                h[N->T.off_w[l] + j] = (float)((2.0 * uniform01(s) - 1.0) * lim);
+        }
+        N->w.ensure(off);
+        N->grad.ensure(off);
+        N->m1.ensure(off);
+        N->m2.ensure(off);
+        N->wb.ensure((size_t)offb);
+        N->err.ensure(1);
+        N->loss_part.ensure(kLossBlocks);
+        NCK(cudaMemcpyAsync(N->w.p, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice, N->stream));
+        NCK(cudaMemsetAsync(N->m1.p, 0, sizeof(float) * off, N->stream));
+        NCK(cudaMemsetAsync(N->m2.p, 0, sizeof(float) * off, N->stream));
+        NCK(cudaMemsetAsync(N->grad.p, 0, sizeof(float) * off, N->stream));
+        NCK(cudaMemsetAsync(N->wb.p, 0, sizeof(bf16) * offb, N->stream));
+        NCK(cudaMemsetAsync(N->err.p, 0, sizeof(int), N->stream));
+        {
+            const std::vector<double> U = unit_solution(side);
+            std::vector<float> Uf(U.begin(), U.end());
+            N->u1.ensure(Uf.size());
+            NCK(cudaMemcpyAsync(N->u1.p, Uf.data(), Uf.size() * sizeof(float), cudaMemcpyHostToDevice, N->stream));
+            NCK(cudaStreamSynchronize(N->stream));  // Uf is a temporary
+        }
+        N->ctas_tc32 = tc_grid<4, 32>(N.get(), &N->info);
+        N->ctas_tc_in = tc_grid<1, 32>(N.get(), &N->info);
+        N->ctas_tc_out = tc_grid<4, 16>(N.get(), &N->info);
+        N->wg_ctas = N->sms * 4;
+        set_wgrad_smem<float, 32, 32, 1>(N->g);
+        set_wgrad_smem<bf16, 32, 32, 32>(N->g);
+        set_wgrad_smem<bf16, 2, 8, 32>(N->g);
+        N->gpart.ensure((size_t)N->wg_ctas * Wgrad<32, 32>::NV);
+        cast_weights(N.get());
+        NCK(cudaStreamSynchronize(N->stream));
+        *out = N.release();
+    });
+}
+
+void dgpu_net_destroy(dgpu_net* net) { delete net; }
+
+int64_t dgpu_net_num_params(const dgpu_net* net) { return net ? net->nparams : 0; }
+
+int dgpu_net_side(const dgpu_net* net) { return net ? net->g.W : 0; }
+
+int dgpu_net_get_params(dgpu_net* net, float* out) {
+    return net_run([&] {
+        check_net(net);
+        if (!out) net_invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        NCK(cudaMemcpyAsync(out, net->w.p, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost, net->stream));
+        NCK(cudaStreamSynchronize(net->stream));
+    });
+}
+
+int dgpu_net_set_params(dgpu_net* net, const float* in) {
+    return net_run([&] {
+        check_net(net);
+        if (!in) net_invalid("buffers must not be NULL");
+        for (int j = 0; j < net->nparams; ++j)
+            if (!std::isfinite(in[j])) net_invalid("parameters must be finite");
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        NCK(cudaMemcpyAsync(net->w.p, in, sizeof(float) * net->nparams, cudaMemcpyHostToDevice, net->stream));
+        NCK(cudaMemsetAsync(net->m1.p, 0, sizeof(float) * net->nparams, net->stream));
+        NCK(cudaMemsetAsync(net->m2.p, 0, sizeof(float) * net->nparams, net->stream));
+        net->step = 0;
+        cast_weights(net);
+        NCK(cudaStreamSynchronize(net->stream));
+    });
+}
+
+int dgpu_net_get_scaling(dgpu_net* net, double* out4) {
+    return net_run([&] {
+        check_net(net);
+        if (!out4) net_invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(net->mu);
+        out4[0] = net->mu_la;
+        out4[1] = net->sd_la;
+        out4[2] = net->uscale;
+        out4[3] = net->fref;
+    });
+}
+
+int dgpu_net_set_scaling(dgpu_net* net, const double* in4) {
+    return net_run([&] {
+        check_net(net);
+        if (!in4) net_invalid("buffers must not be NULL");
+        if (!std::isfinite(in4[0]) || !(in4[1] > 0) || !(in4[2] > 0) || !(in4[3] > 0) || !std::isfinite(in4[1]) ||
+            !std::isfinite(in4[2]) || !std::isfinite(in4[3]))
+            net_invalid("scaling must be finite with sd, uscale and fref > 0");
+        std::lock_guard<std::mutex> lock(net->mu);
+        net->mu_la = in4[0];
+        net->sd_la = in4[1];
+        net->uscale = in4[2];
+        net->fref = in4[3];
+        net->have_scaling = true;
+    });
+}
+
+int dgpu_net_set_engine(dgpu_net* net, int engine) {
+    return net_run([&] {
+        check_net(net);
+        if (engine != DGPU_NET_TENSOR && engine != DGPU_NET_SIMT) net_invalid("unknown engine");
+        std::lock_guard<std::mutex> lock(net->mu);
+        net->engine = engine;
+    });
+}
+
+int dgpu_net_set_loss(dgpu_net* net, int kind) {
+    return net_run([&] {
+        check_net(net);
+        if (kind != DGPU_NET_LOSS_ENERGY && kind != DGPU_NET_LOSS_MSE) net_invalid("unknown loss");
+        std::lock_guard<std::mutex> lock(net->mu);
+        net->loss_kind = kind;
+    });
+}
+
+int dgpu_net_load_pairs(dgpu_net* net, const double* a, const double* u, const double* f, int64_t count) {
+    return net_run([&] {
+        check_net(net);
+        check_samples(a, count);
+        if (!u) net_invalid("buffers must not be NULL");
+        check_f_host(f, count);
+        check_a_host(a, count * (int64_t)net->hw);
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        net->launches = 0;
+        const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)(8 << 20) / net->hw));
+        if (!net->have_scaling) {
+            double fs = 0.0;
+            if (f)
+                for (int64_t q = 0; q < count; ++q) fs += std::fabs(f[q]);
+            net->fref = f ? fs / (double)count : 1.0;
+            // dataset statistics, reduced on the device and summed in a fixed order
+            double s1 = 0, s2 = 0, s3 = 0;
+            std::vector<double> part(kStatBlocks * 3);
+            double* dp = net->stat_part.ensure(kStatBlocks * 3);
+            for (int64_t at = 0; at < count; at += chunk) {
+                const int64_t c = std::min(chunk, count - at);
+                const size_t np = (size_t)c * net->hw;
+                double* da = net->stage_a.ensure(np);
+                double* du = net->stage_u.ensure(np);
+                double* df = f ? net->stage_f.ensure(c) : nullptr;
+                NCK(cudaMemcpyAsync(da, a + at * net->hw, np * 8, cudaMemcpyHostToDevice, net->stream));
+                NCK(cudaMemcpyAsync(du, u + at * net->hw, np * 8, cudaMemcpyHostToDevice, net->stream));
+                if (f) NCK(cudaMemcpyAsync(df, f + at, c * 8, cudaMemcpyHostToDevice, net->stream));
+                k_stats<<<kStatBlocks, 256, 0, net->stream>>>(da, du, df, c, net->hw, net->fref, dp);
+                launched(net);
+                NCK(cudaMemcpyAsync(part.data(), dp, part.size() * 8, cudaMemcpyDeviceToHost, net->stream));
+                NCK(cudaStreamSynchronize(net->stream));
+                for (int q = 0; q < kStatBlocks; ++q) {
+                    s1 += part[3 * q];
+                    s2 += part[3 * q + 1];
+                    s3 += part[3 * q + 2];
+                }
+            }
+            const double n = (double)count * net->hw;
+            const double mu = s1 / n;
+            double sd = std::sqrt(std::max(s2 / n - mu * mu, 0.0));
+            if (!(sd > 1e-12)) sd = 1.0;
+            const double us = std::sqrt(s3 / n);
+            if (!std::isfinite(mu)) net_invalid("permeability must be finite and strictly positive everywhere");
+            if (!(us > 0) || !std::isfinite(us)) net_invalid("solutions must be finite and not all zero");
+            net->mu_la = mu;
+            net->sd_la = sd;
+            net->uscale = us;
+            net->have_scaling = true;
+        }
+        net->ds_x.ensure((size_t)count * net->hw * 8);
+        net->ds_t.ensure((size_t)count * net->hw);
+        net->ds_a.ensure((size_t)count * net->hw);
+        net->ds_norm.ensure((size_t)count);
+        for (int64_t at = 0; at < count; at += chunk) {
+            const int64_t c = std::min(chunk, count - at);
+            featurize_into(net, a + at * net->hw, u + at * net->hw, f ? f + at : nullptr, c, false,
+                           net->ds_x.p + (size_t)at * net->hw * 8, net->ds_t.p + (size_t)at * net->hw,
+                           net->ds_a.p + (size_t)at * net->hw, net->ds_norm.p + at);
+            NCK(cudaStreamSynchronize(net->stream));  // the staging buffers are reused by the next chunk
+        }
+        net->ds_count = count;
+    });
+}
+
+int dgpu_net_train(dgpu_net* net, int64_t steps, int batch, float lr, unsigned long long seed, float* losses) {
+    return net_run([&] {
+        check_net(net);
+        if (steps < 1) net_invalid("steps must be at least 1");
+        if (batch < 1) net_invalid("batch must be at least 1");
+        if (!(lr > 0.f) || !std::isfinite(lr)) net_invalid("learning rate must be positive");
+        std::lock_guard<std::mutex> lock(net->mu);
+        if (net->ds_count < 1) net_invalid("no training pairs loaded");
+        if (batch > net->ds_count) net_invalid("batch larger than the loaded dataset");
+        NCK(cudaSetDevice(net->device));
+        ensure_batch(net, batch, true);
+        net->launches = 0;
+        // sample order: a fresh permutation of the dataset per epoch, fixed by the seed
+        std::vector<int> order((size_t)steps * batch);
+        std::vector<int> perm((size_t)net->ds_count);
+        uint64_t s = seed;
+        size_t pos = perm.size();
+        for (size_t q = 0; q < order.size(); ++q) {
+            if (pos >= perm.size()) {
+                for (size_t j = 0; j < perm.size(); ++j) perm[j] = (int)j;
+                for (size_t j = perm.size() - 1; j > 0; --j) std::swap(perm[j], perm[splitmix(s) % (j + 1)]);
+                pos = 0;
+            }
+            order[q] = perm[pos++];
+        }
+        int* di = net->idx.ensure(order.size());
+        NCK(cudaMemcpyAsync(di, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, net->stream));
+        float* dl = net->losses.ensure((size_t)steps);
+        for (int64_t st = 0; st < steps; ++st) {
+            k_gather<<<grid_for((int64_t)batch * (net->hw + net->hw / 2), 256, net->sms), 256, 0, net->stream>>>(
+                net->ds_x.p, net->ds_t.p, net->ds_a.p, net->ds_norm.p, di + st * batch, batch, net->hw, net->x0.p,
+                net->target.p, net->af.p, net->norm.p);
+            launched(net);
+            forward(net, batch, true);
+            backward(net, batch, dl + st);
+            adam_step(net, lr);
+        }
+        if (losses) NCK(cudaMemcpyAsync(losses, dl, sizeof(float) * steps, cudaMemcpyDeviceToHost, net->stream));
+        check_err(net);
+    });
+}
+
+int dgpu_net_gradients(dgpu_net* net, const double* a, const double* u, const double* f, int64_t count, float* grad,
+                       float* loss) {
+    return net_run([&] {
+        check_net(net);
+        check_samples(a, count);
+        if (!u || !grad) net_invalid("buffers must not be NULL");
+        check_f_host(f, count);
+        check_a_host(a, count * (int64_t)net->hw);
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        if (!net->have_scaling) net_invalid("scaling not set: load pairs or set the scaling first");
+        ensure_batch(net, count, true);
+        net->launches = 0;
+        featurize_into(net, a, u, f, count, false, net->x0.p, net->target.p, net->af.p, net->norm.p);
+        forward(net, count, true);
+        float* dl = net->losses.ensure(1);
+        backward(net, count, dl);
+        NCK(cudaMemcpyAsync(grad, net->grad.p, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost, net->stream));
+        if (loss) NCK(cudaMemcpyAsync(loss, dl, sizeof(float), cudaMemcpyDeviceToHost, net->stream));
+        check_err(net);
+    });
+}
+
+int dgpu_net_features(dgpu_net* net, const double* a, const double* f, int64_t count, float* out) {
+    return net_run([&] {
+        check_net(net);
+        check_samples(a, count);
+        if (!out) net_invalid("buffers must not be NULL");
+        check_f_host(f, count);
+        check_a_host(a, count * (int64_t)net->hw);
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        if (!net->have_scaling) net_invalid("scaling not set: load pairs or set the scaling first");
+        ensure_batch(net, count, false);
+        featurize_into(net, a, nullptr, f, count, false, net->x0.p, nullptr);
+        std::vector<uint16_t> h((size_t)count * net->hw * 8);
+        NCK(cudaMemcpyAsync(h.data(), net->x0.p, h.size() * 2, cudaMemcpyDeviceToHost, net->stream));
+        NCK(cudaStreamSynchronize(net->stream));
+        for (size_t p = 0; p < (size_t)count * net->hw; ++p)
+            for (int c = 0; c < 2; ++c) {
+                const uint32_t bits = (uint32_t)h[p * 8 + c] << 16;
+                float v;
+                std::memcpy(&v, &bits, 4);
+                out[p * 2 + c] = v;
+            }
+    });
+}
+
+int dgpu_net_predict(dgpu_net* net, const double* a, const double* f, int64_t count, double* u0) {
+    return net_run([&] {
+        check_net(net);
+        check_samples(a, count);
+        if (!u0) net_invalid("buffers must not be NULL");
+        check_f_host(f, count);
+        check_a_host(a, count * (int64_t)net->hw);
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        predict_impl(net, a, f, count, u0, false, nullptr);
+    });
+}
+
+int dgpu_net_predict_device(dgpu_net* net, const double* d_a, const double* d_f, int64_t count, double* d_u0,
+                            void* stream) {
+    return net_run([&] {
+        check_net(net);
+        check_samples(d_a, count);
+        if (!d_u0) net_invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(net->mu);
+        NCK(cudaSetDevice(net->device));
+        predict_impl(net, d_a, d_f, count, d_u0, true, (cudaStream_t)stream);
+        NCK(cudaStreamSynchronize(net->stream));
+        if (net_error_pending(net)) throw NetFailure{DGPU_TIMEOUT, "tensor-core convolution: an MMA completion wait ran out"};
+    });
+}
+
+int64_t dgpu_net_last_launches(const dgpu_net* net) { return net ? net->launches : 0; }
+
+int dgpu_net_info(dgpu_net* net, char* out, int capacity) {
+    return net_run([&] {
+        check_net(net);
+        if (!out || capacity < 1) net_invalid("buffers must not be NULL");
+        std::snprintf(out, (size_t)capacity, "side %d, %d parameters; %s", net->g.W, net->nparams, net->info.c_str());
+    });
+}
+
+}  // extern "C"

@@ -772,7 +772,8 @@ size_t smem_budget_for(bool mixed) { return mixed ? 48 * 1024 : 96 * 1024; }
 // host (or device when device_ptrs) packed arrays.
 void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, const std::vector<int64_t>& off,
                  const double* a, const double* f, int f_shared, double fscalar, const double* u0,
-                 const dgpu_options* o, double* u_out, BatchOut out, bool device_ptrs, float* ms_out) {
+                 const dgpu_options* o, double* u_out, BatchOut out, bool device_ptrs, float* ms_out,
+                 const std::function<void(const double*, double*, cudaStream_t)>* warm = nullptr) {
     cudaStream_t s = C->stream;
     const int64_t total = off[count - 1] + (int64_t)sides[count - 1] * sides[count - 1];
     const int maxside = *std::max_element(sides.begin(), sides.end());
@@ -817,6 +818,11 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         CK(cudaMemcpyAsync((void*)A.f, f, sizeof(double) * (f_shared ? (size_t)sides[0] * sides[0] : (size_t)total),
                            in, s));
     if (u0) CK(cudaMemcpyAsync((void*)A.u0, u0, sizeof(double) * total, in, s));
+    if (warm) {  // warm start computed on the device from the resident permeability
+        double* d_u0 = C->bu0.ensure(total);
+        (*warm)(A.a, d_u0, s);
+        A.u0 = d_u0;
+    }
     CK(cudaMemcpyAsync((void*)A.order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)A.side, sides.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)A.off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, s));
@@ -856,7 +862,9 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         // time every candidate on the batch's largest problems
         const int64_t sample = std::min<int64_t>(count, 2 * (int64_t)C->sms);
         float best = 1e30f;
-        for (int threads : {128, 256, 512})
+        // (1024 threads: one problem per SM, half the resident arenas of 2 x 512,
+        // for when the arenas of all resident problems outgrow the L2)
+        for (int threads : {128, 256, 512, 1024})
             for (size_t smem : {(size_t)0, smem_budget_for(mixed)}) {
                 const BlockConfig c{threads, smem};
                 launch(c, sample);  // warm (allocations, clocks)
@@ -1144,6 +1152,34 @@ int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, co
         o.record_history = 0;
         BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
         block_solve(ctx, count, sv, offsets_of(sv), a, f, 0, f_scalar, u0, &o, u_out, bo, false, nullptr);
+    });
+}
+
+int dgpu_solve_batch_learned(dgpu_context* ctx, dgpu_net* net, const double* a, double f_scalar, int64_t batch,
+                             int64_t n, const dgpu_options* opt, double* u_out, int* iterations, double* residuals,
+                             int* converged, int* levels) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        if (!net) invalid("network must not be NULL");
+        check_options(n, opt);
+        if (batch < 1) invalid("a must have shape (batch, n, n)");
+        if (!a || !u_out || !iterations || !residuals || !converged) invalid("buffers must not be NULL");
+        if (net_side(net) != n) invalid("the network was built for another grid side");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        std::vector<int> sides((size_t)batch, (int)n);
+        dgpu_options o = *opt;
+        o.record_history = 0;
+        BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
+        const std::function<void(const double*, double*, cudaStream_t)> warm =
+            [&](const double* d_a, double* d_u0, cudaStream_t s) {
+                std::string msg;
+                const int rc = net_predict_on_stream(net, d_a, f_scalar, batch, d_u0, s, &msg);
+                if (rc != DGPU_OK) throw Failure{rc, msg};
+            };
+        block_solve(ctx, batch, sides, offsets_of(sides), a, nullptr, 1, f_scalar, nullptr, &o, u_out, bo, false,
+                    nullptr, &warm);
+        ctx->last_launches += net_launches(net);
     });
 }
 

@@ -162,6 +162,72 @@ int dgpu_apply_preconditioner_noalloc(const double* d_a, const double* d_r, int6
  * timed runs). */
 int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes);
 
+/* ------------------------------------------------------------------------
+ * Learned warm start. No counterpart in the reference (which always starts
+ * PCG from u0 = 0, solver.hpp:96-102): a 6-layer 3x3 convolutional network
+ * (2 -> 32 x 5 -> 1 channels, GELU, BF16 weights and activations, FP32
+ * accumulation) maps (log a, f) on a side x side grid to a guess of u, which
+ * the solve then refines to the same tolerance. Training data are (a, u)
+ * pairs the solver produced (for example dgpu_solve_batch at tol 1e-10).
+ * One network per grid side (even, 8..512).
+ * Parameters are one FP32 vector: per layer l, w_l[cout][tap * cin + ci]
+ * (tap = 3 * (dy + 1) + (dx + 1)), then b_l[cout]. Training minimises the
+ * prediction's error in the energy norm of each sample's own operator (the
+ * norm CG minimises), relative to the solution's, unless set otherwise. */
+typedef struct dgpu_net dgpu_net;
+
+#define DGPU_NET_TENSOR 0 /* 32 -> 32 convolutions on the tensor cores (default) */
+#define DGPU_NET_SIMT 1   /* same arithmetic on the CUDA cores (cross-check)      */
+
+/* New network on the current device, He-uniform weights from `seed`. */
+int dgpu_net_create(int side, unsigned long long seed, dgpu_net** out);
+void dgpu_net_destroy(dgpu_net* net);
+int64_t dgpu_net_num_params(const dgpu_net* net);
+int dgpu_net_side(const dgpu_net* net);
+int dgpu_net_get_params(dgpu_net* net, float* out);
+/* Replaces the parameters and resets the Adam moments. */
+int dgpu_net_set_params(dgpu_net* net, const float* in);
+/* Input/output scaling {mean of log a, std of log a, RMS of u at f = fref,
+ * fref}; set by the first dgpu_net_load_pairs unless set here first. */
+int dgpu_net_get_scaling(dgpu_net* net, double* out4);
+int dgpu_net_set_scaling(dgpu_net* net, const double* in4);
+int dgpu_net_set_engine(dgpu_net* net, int engine);
+
+#define DGPU_NET_LOSS_ENERGY 0 /* e^T A e / u^T A u per sample, batch mean (default) */
+#define DGPU_NET_LOSS_MSE 1    /* mean of (u0 - u)^2 over all cells, u scaled to unit RMS */
+int dgpu_net_set_loss(dgpu_net* net, int kind);
+/* Host arrays: a and u packed (count, side, side); f NULL (f = 1) or one
+ * scalar forcing per sample. Replaces the resident training set. */
+int dgpu_net_load_pairs(dgpu_net* net, const double* a, const double* u, const double* f, int64_t count);
+/* `steps` Adam steps (betas 0.9 / 0.999, eps 1e-8) on mini-batches drawn
+ * without replacement from the resident set (a new permutation per epoch,
+ * fixed by `seed`); the loss of each step goes to losses[steps] (may be NULL). */
+int dgpu_net_train(dgpu_net* net, int64_t steps, int batch, float lr, unsigned long long seed, float* losses);
+/* The loss and its gradient with respect to every parameter for one batch
+ * of host samples (no update). */
+int dgpu_net_gradients(dgpu_net* net, const double* a, const double* u, const double* f, int64_t count,
+                       float* grad, float* loss);
+/* The network's input for `count` samples, as it enters the first layer
+ * (after BF16 rounding): out[count][side][side][2] = ((log a - mean) / std,
+ * (f / fref) U1) where U1 is the grid's a = 1, f = 1 solution at unit RMS. */
+int dgpu_net_features(dgpu_net* net, const double* a, const double* f, int64_t count, float* out);
+/* u0 for `count` samples (host arrays). */
+int dgpu_net_predict(dgpu_net* net, const double* a, const double* f, int64_t count, double* u0);
+/* Same on device arrays, ordered after / before `stream` (may be NULL). */
+int dgpu_net_predict_device(dgpu_net* net, const double* d_a, const double* d_f, int64_t count, double* d_u0,
+                            void* stream);
+/* Kernels launched by the network's last call. */
+int64_t dgpu_net_last_launches(const dgpu_net* net);
+/* Text description of the network and its launch shapes. */
+int dgpu_net_info(dgpu_net* net, char* out, int capacity);
+
+/* dgpu_solve_batch with the warm start predicted on the device by `net`
+ * (whose side must equal n): the prediction never leaves the GPU. f is the
+ * scalar f_scalar for every sample. */
+int dgpu_solve_batch_learned(dgpu_context* ctx, dgpu_net* net, const double* a, double f_scalar, int64_t batch,
+                             int64_t n, const dgpu_options* opt, double* u_out, int* iterations, double* residuals,
+                             int* converged, int* levels);
+
 #ifdef __cplusplus
 }
 #endif
