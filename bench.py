@@ -36,6 +36,11 @@ METRIC = "64² solves/s & 1024² ms/solve at rel-res 1e-10: chosen form vs plain
 N_BIG, SEED_BIG, HI_BIG, LO_BIG = 1024, 1, 1e3, 1e-3
 N_SMALL, BATCH_SMALL = 64, 4096
 TOL = 1e-10
+# learned warm start at 64 x 64: pairs generated by the GPU solver from seeds
+# 10000..29999, Adam lr 1e-3 batch 256, held-out evaluation seeds 30000..31999
+LEARN_TRAIN_SEEDS = range(10000, 30000)
+LEARN_EVAL_SEEDS = range(30000, 32000)
+LEARN_EPOCHS = 4
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
 
@@ -105,6 +110,22 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- GPU (ours)
+
+def load_traffic(kernel: str, workload: str) -> float | None:
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summary table (profiles/dram_traffic.md), or None."""
+    path = ROOT / "profiles" / "dram_traffic.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) >= 3 and cells[0] == kernel and cells[1] == workload:
+            try:
+                return float(cells[2])
+            except ValueError:
+                return None
+    return None
+
 
 def load_peaks() -> dict:
     path = ROOT / "MEASURED_PEAKS.json"
@@ -186,6 +207,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                 br = darcy.solve_batch(batch, tol=TOL, form=form)
                 runs.append(time.perf_counter() - t0)
             bt[form] = (min(runs), br)
+        learned = run_learned(batch, flush)
     total_ms = {k: sum(v) for k, v in times.items()}
     if world > 1:
         t = torch.tensor([total_ms["mixed"], total_ms["fp64"]], device=f"cuda:{dev}")
@@ -207,8 +229,10 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     peaks = load_peaks()
     dom = max(prof, key=lambda k: k["share_ms"])
     achieved = dom["bytes"] / (dom["avg_ms"] * 1e-3) / 1e9
+    traffic = load_traffic(dom["name"], "1024x1024 mixed")
     roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                "traffic_source": "profiles/dram_traffic.md (ncu, cold L2, one launch)" if traffic else None,
                 "peak_source": peaks["source"], "avg_launch_us": round(dom["avg_ms"] * 1e3, 3),
                 "algorithmic_bytes_per_launch": dom["bytes"],
                 "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()} for p in prof]}
@@ -242,7 +266,11 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                     "mixed": round(bsm, 1), "fp64": round(bsp, 1), "unit": "solves/s",
                     "chosen_vs_plain": round(bsm / bsp, 3),
                     "mean_iterations": float(bt["mixed"][1].iterations.mean()),
-                    "e2e": True, "h2d_bytes": int(batch.nbytes), "d2h_bytes": int(batch.nbytes)},
+                    "e2e": True, "h2d_bytes": int(batch.nbytes), "d2h_bytes": int(batch.nbytes),
+                    "mixed_learned": learned["solves_per_s"],
+                    "learned_vs_plain": round(learned["solves_per_s"] / bsp, 3),
+                    "learned_mean_iterations": learned["mean_iterations"]},
+        "learned": learned,
         "e2e": {"value": round(e2e_mixed, 3), "unit": "ms/solve", "h2d_bytes_per_step": int(8 * m),
                 "d2h_bytes_per_step": int(8 * m + 64)},
         "gpu_launches": int(st_m.kernel_launches),
@@ -251,6 +279,52 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "clocks": clocks.summary(),
     }
     return line
+
+
+def run_learned(batch: np.ndarray, flush) -> dict:
+    """Trains the warm-start network on solver-generated 64 x 64 pairs, then
+    times the batched mixed solve with the predicted start (prediction on the
+    device, inside the timed call) and compares iterations on held-out fields."""
+    import torch
+
+    import darcy_cpp_gb300 as darcy
+    from darcy_cpp_gb300 import learn
+
+    t0 = time.perf_counter()
+    a_tr, u_tr = learn.generate_pairs(LEARN_TRAIN_SEEDS, N_SMALL)
+    gen_s = time.perf_counter() - t0
+    net = learn.WarmStartNet(N_SMALL, seed=0)
+    steps = LEARN_EPOCHS * len(LEARN_TRAIN_SEEDS) // 256
+    t0 = time.perf_counter()
+    losses = net.fit(a_tr, u_tr, steps=steps, batch=256, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    held = learn.permeability_fields(LEARN_EVAL_SEEDS, N_SMALL)
+    zero = darcy.solve_batch(held, tol=TOL, form="mixed")
+    warm = learn.solve_batch_learned(net, held, tol=TOL, form="mixed")
+    ref = darcy.solve_batch(held[:64], tol=TOL, form="fp64")
+    u0 = net.predict(held[:64])
+    u0_err = float(np.mean([np.linalg.norm(u0[q] - ref.u[q]) / np.linalg.norm(ref.u[q]) for q in range(64)]))
+    sol_err = float(max(np.linalg.norm(warm.u[q] - ref.u[q]) / np.linalg.norm(ref.u[q]) for q in range(64)))
+    learn.solve_batch_learned(net, batch[:256], tol=TOL, form="mixed")
+    runs = []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = learn.solve_batch_learned(net, batch, tol=TOL, form="mixed")
+        runs.append(time.perf_counter() - t0)
+    return {"solves_per_s": round(BATCH_SMALL / min(runs), 1), "mean_iterations": float(r.iterations.mean()),
+            "all_converged": bool(r.all_converged),
+            "heldout": {"seeds": f"{LEARN_EVAL_SEEDS.start}..{LEARN_EVAL_SEEDS.stop - 1}",
+                        "mean_iterations_zero_start": float(zero.iterations.mean()),
+                        "mean_iterations_learned_start": float(warm.iterations.mean()),
+                        "u0_rel_l2_vs_solution": round(u0_err, 4),
+                        "solution_rel_l2_vs_fp64": sol_err},
+            "training": {"pairs": len(LEARN_TRAIN_SEEDS), "pair_generation_s": round(gen_s, 2),
+                         "steps": steps, "batch": 256, "lr": 1e-3, "seconds": round(train_s, 2),
+                         "loss_first": float(losses[0]), "loss_last": float(np.mean(losses[-20:])),
+                         "loss": "energy norm of u0 - u relative to u"},
+            "net": net.handle.info()}
 
 
 # ------------------------------------------------------- CPU (the oracle)

@@ -53,7 +53,10 @@ struct Failure {
 [[noreturn]] void invalid(const std::string& msg) { throw Failure{DGPU_INVALID_INPUT, msg}; }
 
 // Grid-engine cut-off: the levels of side <= kTailSide form the coarse tail,
-// applied as one dense matrix (precomputed at setup) per visit.
+// applied as one dense matrix (precomputed at setup) per visit. (A 64-side
+// tail for the FP32 cycle -- a 64 MB operator that stays in L2 -- measured
+// slower at 1024^2: 44.5 against 38.9 ms, its 4096-column setup and 64 MB
+// products outweighing the launches it saves.)
 constexpr int kTailSide = 32;
 constexpr int kChunk = 8;  // iterations per launch when conditional nodes are unavailable
 
@@ -235,6 +238,7 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
     P.m = (int64_t)K.n * K.n;
     const std::vector<int> sides = level_sides(K.n);
     P.nlev = (int)sides.size();
+    P.mixed_mg = K.form == DGPU_FORM_MIXED && K.pc == kPcMultigrid;
     P.tail_l0 = P.nlev - 1;
     for (int l = 0; l < P.nlev; ++l)
         if (sides[l] <= kTailSide) {
@@ -242,7 +246,6 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
             break;
         }
     P.ntail = sides[P.tail_l0] * sides[P.tail_l0];
-    P.mixed_mg = K.form == DGPU_FORM_MIXED && K.pc == kPcMultigrid;
     const size_t m = (size_t)P.m;
     P.h.assign(P.nlev, Lvl64{});
     P.lvd.assign(P.nlev, Lvl<double>{});
