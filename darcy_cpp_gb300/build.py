@@ -71,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> tuple[Path, Path]:
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
     headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [INCLUDE / "darcy_gpu.h"]
-    units = ["kernels", "solver", "noalloc", "learn"]
+    units = ["kernels", "solver", "noalloc", "learn", "fieldgen"]
     units = [u for u in units if (CSRC / f"{u}.cu").exists()]
     objs = [BUILD / f"{u}.o" for u in units]
     flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -79,6 +79,9 @@ def lib() -> ctypes.CDLL:
         L.dgpu_flush_l2.argtypes = [_P, ctypes.c_int64]
         L.dgpu_apply_preconditioner_noalloc.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                                         ctypes.c_int, _P, _P]
+        L.dgpu_random_fields.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_ulonglong, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, _P,
+                                         ctypes.c_int, _P]
         # learned warm start
         L.dgpu_net_create.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_P)]
         L.dgpu_net_destroy.argtypes = [_P]
@@ -137,6 +140,16 @@ def apply_preconditioner_noalloc(d_a: int, d_r: int, n: int, d_z: int, pre_sweep
     check(lib().dgpu_apply_preconditioner_noalloc(ctypes.c_void_p(d_a), ctypes.c_void_p(d_r), int(n), int(pre_sweeps),
                                                   int(post_sweeps), int(cycle_index), ctypes.c_void_p(d_z),
                                                   ctypes.c_void_p(stream) if stream else None))
+
+
+def random_fields(n: int, count: int, seed: int = 0, alpha: float = 2.0, tau: float = 3.0, hi: float = 12.0,
+                  lo: float = 3.0, raw: bool = False) -> np.ndarray:
+    """`count` two-phase fields (or raw Gaussian fields) generated on the GPU
+    (dgpu_random_fields; same distribution as the host generator, other bits)."""
+    out = np.empty((int(count), int(n), int(n)))
+    check(lib().dgpu_random_fields(int(n), int(count), int(seed) & ((1 << 64) - 1), float(alpha), float(tau),
+                                   float(hi), float(lo), int(bool(raw)), _ptr(out), 0, None))
+    return out
 
 
 class Context:
@@ -201,6 +214,30 @@ class Context:
         check(lib().dgpu_solve_batch(self.handle, _ptr(a), _ptr(fa), float(f) if fa is None else 0.0, 0, batch, n,
                                      ctypes.byref(opt), None, _ptr(u), _ptr(it), _ptr(res), _ptr(conv), _ptr(lev)))
         return {"u": u, "iterations": it, "residuals": res, "converged": conv.astype(bool), "levels": lev}
+
+    def solve_uneven(self, fields, f=None, x0=None, f_scalar: float = 1.0, **kw) -> dict:
+        """Problems of different sides in one call (dgpu_solve_uneven); f and
+        x0 are None or one array per problem."""
+        arrays = [_f64(x) for x in fields]
+        sides = np.array([x.shape[0] for x in arrays], dtype=np.int64)
+        a = np.concatenate([x.ravel() for x in arrays])
+        fa = None if f is None else np.concatenate([_f64(x).ravel() for x in f])
+        u0 = None if x0 is None else np.concatenate([_f64(x).ravel() for x in x0])
+        u = np.empty_like(a)
+        count = len(arrays)
+        it = np.zeros(count, dtype=np.int32)
+        res = np.zeros(count)
+        conv = np.zeros(count, dtype=np.int32)
+        lev = np.zeros(count, dtype=np.int32)
+        opt = options(**kw)
+        check(lib().dgpu_solve_uneven(self.handle, count, _ptr(sides), _ptr(a), _ptr(fa), float(f_scalar),
+                                      ctypes.byref(opt), _ptr(u0), _ptr(u), _ptr(it), _ptr(res), _ptr(conv),
+                                      _ptr(lev)))
+        out, at = [], 0
+        for n in sides:
+            out.append(u[at:at + n * n].reshape(n, n))
+            at += n * n
+        return {"u": out, "iterations": it, "residuals": res, "converged": conv.astype(bool), "levels": lev}
 
     def apply_operator(self, a, x) -> np.ndarray:
         a, x = _f64(a), _f64(x)

@@ -26,6 +26,7 @@
 
 #include "../../include/darcy_gpu.h"
 #include "engine.h"
+#include "cluster.cuh"
 
 using namespace dgpu;
 
@@ -158,6 +159,7 @@ struct GridPlan {
     int ntail = 0;                  // cells of the first tail level (dense operator is ntail x ntail)
     int64_t m = 0;
     bool mixed_mg = false;
+    int cl0 = -1, cl_nl = 0, cl_ctas = 0;  // coarse levels run by one thread-block cluster (cl0 = top), or -1
     Arena arena;
     double *a = nullptr, *f = nullptr, *u0 = nullptr, *u = nullptr;
     double *b = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr;
@@ -206,6 +208,10 @@ struct dgpu_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
     bool cond_ok = false;
+    bool host_direct = false;  // kernels may read/write pageable host arrays (ATS over NVLink-C2C)
+    cudaStream_t copy_stream = nullptr;  // host<->device copies of pipelined batches
+    cudaStream_t stream2 = nullptr;      // second compute stream of pipelined batches
+    std::vector<cudaEvent_t> chunk_events;
     int sms = 0;
     std::string info;
     std::map<PlanKey, std::unique_ptr<GridPlan>> plans;
@@ -215,7 +221,7 @@ struct dgpu_context {
     DVec<int64_t> boff;
     DVec<unsigned long long> bbad;
     DVec<unsigned> bwork;
-    DVec<char> bscratch;
+    DVec<char> bscratch, bscratch2;  // per-CTA arenas of the two compute streams of a pipelined batch
     DVec<char> flush;
     // apply_operator / hierarchy buffers
     DVec<char> misc;
@@ -245,6 +251,45 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
             P.tail_l0 = l;
             break;
         }
+    // Coarse levels in one cluster (fused visits only, opt-in with
+    // DARCY_GPU_CLUSTER=1): the first level below the finest with side <= 128
+    // is the cluster's top, the first level with side <= 16 its dense tail.
+    // Measured on GB300 at 1024^2: 83.8 / 74.4 ms (FP64 / mixed) against 46.1 /
+    // 38.4 ms with one launch per visit -- each of the ~78 cluster-barrier
+    // phases of a launch costs ~1.9 us, more than the launches it replaces.
+    P.cl0 = -1;
+    {
+        const char* ce = std::getenv("DARCY_GPU_CLUSTER");
+        const bool want = K.pre == 1 && K.post == 1 && K.pc == kPcMultigrid && ce && std::strcmp(ce, "1") == 0;
+        int top = -1, tl = -1;
+        for (int l = 1; l < P.nlev && top < 0; ++l)
+            if (sides[l] <= kClusterTopRows * kClusterMaxCtas) top = l;
+        for (int l = 0; l < P.nlev && tl < 0; ++l)
+            if (sides[l] <= 16) tl = l;
+        if (want && top >= 1 && tl > top && tl - top <= kClusterMaxLevels) {
+            const int ctas = (sides[top] + kClusterTopRows - 1) / kClusterTopRows;
+            bool ok;
+            if (P.mixed_mg) {
+                ClusterArgs<float> probe{};
+                probe.nl = tl - top;
+                for (int i = 0; i < probe.nl; ++i) probe.lv[i].n = sides[top + i];
+                probe.n_tail = sides[tl];
+                ok = cluster_cycle_supported<float>(probe, ctas);
+            } else {
+                ClusterArgs<double> probe{};
+                probe.nl = tl - top;
+                for (int i = 0; i < probe.nl; ++i) probe.lv[i].n = sides[top + i];
+                probe.n_tail = sides[tl];
+                ok = cluster_cycle_supported<double>(probe, ctas);
+            }
+            if (ok) {
+                P.cl0 = top;
+                P.cl_nl = tl - top;
+                P.cl_ctas = ctas;
+                P.tail_l0 = tl;
+            }
+        }
+    }
     P.ntail = sides[P.tail_l0] * sides[P.tail_l0];
     const size_t m = (size_t)P.m;
     P.h.assign(P.nlev, Lvl64{});
@@ -419,6 +464,18 @@ void emit_visit_fused(GridPlan& P, int l, bool first, std::vector<int>& cur, cud
     }
     if (l + 1 >= P.tail_l0) {
         launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, X(l + 1, 0), P.st, s);
+        cur[l + 1] = 0;
+    } else if (l + 1 == P.cl0) {  // the whole coarse-grid correction in one cluster launch
+        ClusterArgs<T> CA{};
+        CA.nl = P.cl_nl;
+        for (int i = 0; i < P.cl_nl; ++i) CA.lv[i] = visit_level<T>(P, P.cl0 + i);
+        CA.n_tail = P.h[P.tail_l0].n;
+        CA.tail = tail_matrix<T>(P);
+        CA.b_top = lv[l + 1].b;
+        CA.x_top = X(l + 1, 0);
+        CA.gamma = K.gamma;
+        CA.top_calls = K.gamma;
+        launch_cluster_cycle<T>(CA, P.cl_ctas, s);
         cur[l + 1] = 0;
     } else {
         for (int g = 0; g < K.gamma; ++g) emit_visit_fused<T>(P, l + 1, g == 0, cur, s);
@@ -771,6 +828,16 @@ void save_tuning(dgpu_context* C) {
 // chip with two CTAs per SM.
 size_t smem_budget_for(bool mixed) { return mixed ? 48 * 1024 : 96 * 1024; }
 
+// Autotuning key of a batch (loads the tuning file on first use).
+std::string tune_key(dgpu_context* C, int maxside, bool mixed, const dgpu_options* o) {
+    char keybuf[160];
+    std::snprintf(keybuf, sizeof keybuf, "%s|side<=%d|%s|pc%d|c%d|s%d%d", C->device_name.c_str(),
+                  size_bucket(maxside), mixed ? "mixed" : "fp64", o->preconditioner, o->cycle_index,
+                  o->pre_sweeps, o->post_sweeps);
+    load_tuning(C);
+    return keybuf;
+}
+
 // Packed problems through the block engine. sides/off on the host; a, f, u0
 // host (or device when device_ptrs) packed arrays.
 void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, const std::vector<int64_t>& off,
@@ -788,15 +855,18 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sides[x] > sides[y]; });
 
+    // host arrays read and written by the kernel itself (no staging copies)
+    const bool direct = C->host_direct && !device_ptrs;
     BatchArgs A{};
     A.count = (int)count;
-    A.a = C->ba.ensure(total);
+    A.a = direct ? a : C->ba.ensure(total);
     A.u = C->bu.ensure(total);
+    A.u_host = direct ? u_out : nullptr;
     A.f = nullptr;
-    if (f) A.f = C->bf.ensure(f_shared ? (size_t)sides[0] * sides[0] : (size_t)total);
+    if (f) A.f = direct ? f : C->bf.ensure(f_shared ? (size_t)sides[0] * sides[0] : (size_t)total);
     A.f_shared = f_shared;
     A.fscalar = fscalar;
-    A.u0 = u0 ? C->bu0.ensure(total) : nullptr;
+    A.u0 = u0 ? (direct ? u0 : C->bu0.ensure(total)) : nullptr;
     A.order = C->border.ensure(count);
     A.side = C->bside.ensure(count);
     A.off = C->boff.ensure(count);
@@ -806,7 +876,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     A.levels = C->blev.ensure(count);
     A.true_residual = C->btrue.ensure(count);
     A.bad = C->bbad.ensure(count);
-    A.work = C->bwork.ensure(1);
+    A.work = C->bwork.ensure(2);
     A.history = (o->record_history && count == 1) ? C->bhist.ensure((size_t)o->max_iter + 1) : nullptr;
     A.record_history = o->record_history;
     A.tol = o->tol;
@@ -816,11 +886,38 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     A.post = o->post_sweeps;
     A.gamma = o->cycle_index;
 
-    CK(cudaMemcpyAsync((void*)A.a, a, sizeof(double) * total, in, s));
-    if (f)
-        CK(cudaMemcpyAsync((void*)A.f, f, sizeof(double) * (f_shared ? (size_t)sides[0] * sides[0] : (size_t)total),
-                           in, s));
-    if (u0) CK(cudaMemcpyAsync((void*)A.u0, u0, sizeof(double) * total, in, s));
+    // Pipelined host copies for a large batch whose launch shape is already
+    // tuned: the problems are split into a few chunks; chunk k + 1 is copied
+    // in (copy stream) while chunk k runs, and each chunk's solutions are
+    // copied out while the later chunks run.
+    const auto tuned_hit = C->tuned.find(tune_key(C, maxside, mixed, o));
+    const int64_t resident = 2 * (int64_t)C->sms;
+    const bool pipelined = !direct && !device_ptrs && !warm && tuned_hit != C->tuned.end() &&
+                           count >= 4 * resident && !(o->record_history);
+    std::vector<int64_t> cut{0, count};
+    if (pipelined) {
+        const int64_t nchunks = std::min<int64_t>(4, count / (2 * resident));
+        cut.assign(1, 0);
+        for (int64_t k = 1; k <= nchunks; ++k) cut.push_back(count * k / nchunks);
+        // largest first within each chunk
+        for (size_t k = 0; k + 1 < cut.size(); ++k) {
+            std::iota(order.begin() + cut[k], order.begin() + cut[k + 1], (int)cut[k]);
+            std::stable_sort(order.begin() + cut[k], order.begin() + cut[k + 1],
+                             [&](int x, int y) { return sides[x] > sides[y]; });
+        }
+    }
+    auto cells_of = [&](int64_t p0, int64_t p1) -> std::pair<int64_t, int64_t> {
+        const int64_t lo = off[p0];
+        const int64_t hi = off[p1 - 1] + (int64_t)sides[p1 - 1] * sides[p1 - 1];
+        return {lo, hi - lo};
+    };
+    if (!direct && !pipelined) {
+        CK(cudaMemcpyAsync((void*)A.a, a, sizeof(double) * total, in, s));
+        if (f)
+            CK(cudaMemcpyAsync((void*)A.f, f,
+                               sizeof(double) * (f_shared ? (size_t)sides[0] * sides[0] : (size_t)total), in, s));
+        if (u0) CK(cudaMemcpyAsync((void*)A.u0, u0, sizeof(double) * total, in, s));
+    }
     if (warm) {  // warm start computed on the device from the resident permeability
         double* d_u0 = C->bu0.ensure(total);
         (*warm)(A.a, d_u0, s);
@@ -830,31 +927,30 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     CK(cudaMemcpyAsync((void*)A.side, sides.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)A.off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, s));
 
-    // launch with a given shape over the first `n_prob` entries of `order`
-    auto launch = [&](const BlockConfig& cfg, int64_t n_prob) {
+    // launch with a given shape over `n_prob` entries of `order` from `first`
+    // (slot 1: the second compute stream, its own arenas and work counter)
+    auto launch = [&](const BlockConfig& cfg, int64_t n_prob, int64_t first = 0, int slot = 0) {
         const int per_sm = mixed ? block_solve_occupancy<float>(cfg.threads, cfg.smem)
                                  : block_solve_occupancy<double>(cfg.threads, cfg.smem);
         const int ctas = (int)std::min<int64_t>(n_prob, (int64_t)C->sms * std::max(per_sm, 1));
         const size_t stride = align_up(block_arena_bytes(maxside, mixed, cfg.smem));
+        cudaStream_t ls = slot ? C->stream2 : s;
         BatchArgs B = A;
         B.count = (int)n_prob;
-        B.scratch = C->bscratch.ensure(stride * ctas);
+        B.order = A.order + first;
+        B.scratch = (slot ? C->bscratch2 : C->bscratch).ensure(stride * ctas);
         B.scratch_stride = stride;
         B.smem_budget = cfg.smem;
-        CK(cudaMemsetAsync(B.work, 0, sizeof(unsigned), s));
+        B.work = A.work + slot;
+        CK(cudaMemsetAsync(B.work, 0, sizeof(unsigned), ls));
         if (mixed)
-            launch_block_solve<float>(B, ctas, cfg.threads, s);
+            launch_block_solve<float>(B, ctas, cfg.threads, ls);
         else
-            launch_block_solve<double>(B, ctas, cfg.threads, s);
+            launch_block_solve<double>(B, ctas, cfg.threads, ls);
         CK(cudaGetLastError());
     };
 
-    char keybuf[160];
-    std::snprintf(keybuf, sizeof keybuf, "%s|side<=%d|%s|pc%d|c%d|s%d%d", C->device_name.c_str(),
-                  size_bucket(maxside), mixed ? "mixed" : "fp64", o->preconditioner, o->cycle_index,
-                  o->pre_sweeps, o->post_sweeps);
-    const std::string key = keybuf;
-    load_tuning(C);
+    const std::string key = tune_key(C, maxside, mixed, o);
     BlockConfig cfg;
     cfg.smem = smem_budget_for(mixed);
     auto hit = C->tuned.find(key);
@@ -889,8 +985,44 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     C->last_block_smem = cfg.smem;
 
     CK(cudaEventRecord(C->ev0, s));
-    launch(cfg, count);
-    CK(cudaMemcpyAsync(u_out, A.u, sizeof(double) * total, outk, s));
+    if (pipelined) {
+        const size_t nch = cut.size() - 1;
+        while (C->chunk_events.size() < 2 * nch) {
+            cudaEvent_t ev;
+            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            C->chunk_events.push_back(ev);
+        }
+        cudaStream_t cs = C->copy_stream;
+        if (f && f_shared)
+            CK(cudaMemcpyAsync((void*)A.f, f, sizeof(double) * (size_t)sides[0] * sides[0], in, cs));
+        // chunks alternate between the two compute streams so that the next
+        // chunk's CTAs fill the SMs the previous chunk's last wave leaves idle
+        CK(cudaEventRecord(C->chunk_events[0], s));  // order after the uploads above
+        CK(cudaStreamWaitEvent(C->stream2, C->chunk_events[0], 0));
+        for (size_t k = 0; k < nch; ++k) {
+            const auto [lo, len] = cells_of(cut[k], cut[k + 1]);
+            const int slot = (int)(k & 1);
+            cudaStream_t ks = slot ? C->stream2 : s;
+            CK(cudaMemcpyAsync((void*)(A.a + lo), a + lo, sizeof(double) * len, in, cs));
+            if (f && !f_shared) CK(cudaMemcpyAsync((void*)(A.f + lo), f + lo, sizeof(double) * len, in, cs));
+            if (u0) CK(cudaMemcpyAsync((void*)(A.u0 + lo), u0 + lo, sizeof(double) * len, in, cs));
+            CK(cudaEventRecord(C->chunk_events[2 * k], cs));
+            CK(cudaStreamWaitEvent(ks, C->chunk_events[2 * k], 0));
+            launch(cfg, cut[k + 1] - cut[k], cut[k], slot);
+            CK(cudaEventRecord(C->chunk_events[2 * k + 1], ks));
+        }
+        for (size_t k = 0; k < nch; ++k) {
+            const auto [lo, len] = cells_of(cut[k], cut[k + 1]);
+            CK(cudaStreamWaitEvent(cs, C->chunk_events[2 * k + 1], 0));
+            CK(cudaMemcpyAsync(u_out + lo, A.u + lo, sizeof(double) * len, outk, cs));
+        }
+        // the results below are read on the main stream after every chunk and copy
+        CK(cudaEventRecord(C->chunk_events[2 * nch - 1], cs));
+        CK(cudaStreamWaitEvent(s, C->chunk_events[2 * nch - 1], 0));
+    } else {
+        launch(cfg, count);
+        if (!direct) CK(cudaMemcpyAsync(u_out, A.u, sizeof(double) * total, outk, s));
+    }
     std::vector<unsigned long long> bad(count);
     CK(cudaMemcpyAsync(bad.data(), A.bad, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(out.iterations, A.iterations, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
@@ -908,7 +1040,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         CK(cudaMemcpy(out.history, A.history, sizeof(double) * len, cudaMemcpyDeviceToHost));
     }
     if (ms_out) CK(cudaEventElapsedTime(ms_out, C->ev0, C->ev1));
-    C->last_launches = 1;
+    C->last_launches = (int64_t)cut.size() - 1;
 }
 
 }  // namespace
@@ -1068,12 +1200,26 @@ int dgpu_create(int device, dgpu_context** out) {
         C->cond_ok = !(loop && std::strcmp(loop, "host") == 0) && conditional_nodes_work(C->stream);
         const char* pdl = std::getenv("DARCY_GPU_PDL");
         set_programmatic_launch(!(pdl && std::strcmp(pdl, "0") == 0));
+        // Host arrays addressed directly by the batched kernel (opt-in,
+        // DARCY_GPU_HOST_DIRECT=1), only where the device reads pageable
+        // memory through the host's own page tables. Measured on GB300 + Grace:
+        // 3x slower than the pipelined copies for 4096 x 64^2 (34.5 against
+        // 11.1 ms with one CG iteration), so the copies are the default.
+        int pageable = 0, host_tables = 0;
+        CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device));
+        CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device));
+        const char* direct = std::getenv("DARCY_GPU_HOST_DIRECT");
+        C->host_direct = pageable == 1 && host_tables == 1 && direct && std::strcmp(direct, "1") == 0;
+        CK(cudaStreamCreateWithFlags(&C->copy_stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&C->stream2, cudaStreamNonBlocking));
         char buf[512];
         std::snprintf(buf, sizeof buf,
-                      "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s | programmatic launch: %s",
+                      "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s | programmatic launch: %s"
+                      " | batch host arrays: %s",
                       prop.name, prop.multiProcessorCount, prop.major, prop.minor,
                       prop.totalGlobalMem / 1073741824.0, prop.l2CacheSize / 1048576.0,
-                      C->cond_ok ? "device-side" : "host-chunked", programmatic_launch() ? "on" : "off");
+                      C->cond_ok ? "device-side" : "host-chunked", programmatic_launch() ? "on" : "off",
+                      C->host_direct ? "addressed directly" : "copied");
         C->info = buf;
         *out = C.release();
     });
@@ -1088,6 +1234,9 @@ void dgpu_destroy(dgpu_context* ctx) {
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
         if (ctx->ev1) cudaEventDestroy(ctx->ev1);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+        if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+        for (cudaEvent_t ev : ctx->chunk_events) cudaEventDestroy(ev);
     }
     delete ctx;
 }

@@ -21,7 +21,7 @@ import numpy as np
 
 from .fields import gaussian_random_field, two_phase_permeability
 
-__all__ = ["draw_fields", "generate", "main"]
+__all__ = ["draw_fields", "draw_fields_gpu", "generate", "main"]
 
 
 def draw_fields(n_samples: int, grid: int, seed: int = 0, alpha: float = 2.0, tau: float = 3.0) -> np.ndarray:
@@ -33,16 +33,31 @@ def draw_fields(n_samples: int, grid: int, seed: int = 0, alpha: float = 2.0, ta
     return a
 
 
+def draw_fields_gpu(n_samples: int, grid: int, seed: int = 0, alpha: float = 2.0, tau: float = 3.0,
+                    hi: float = 12.0, lo: float = 3.0) -> np.ndarray:
+    """The same construction generated on the GPU (grid <= 128): same
+    distribution as draw_fields, a different random stream."""
+    from .capi import random_fields
+
+    return random_fields(grid, n_samples, seed, alpha, tau, hi, lo)
+
+
 def generate(n_samples: int = 1000, grid: int = 64, seed: int = 0, alpha: float = 2.0, tau: float = 3.0,
              f: float = 1.0, tol: float = 1e-10, max_iter: int = 10000, preconditioner: str = "multigrid",
-             form: str = "fp64", dtype: str = "float32", output: str | Path | None = None) -> dict:
+             form: str = "fp64", dtype: str = "float32", output: str | Path | None = None,
+             gpu_fields: bool = False) -> dict:
     """Draws the fields, solves them on the GPU and (optionally) writes the npz.
 
-    Returns a dict with a, u (float64), iterations and the solve time.
+    gpu_fields draws the fields on the GPU as well (not the reference's
+    random stream). Returns a dict with a, u (float64), iterations and the
+    solve time.
     """
     from . import solve_batch
 
-    a = draw_fields(n_samples, grid, seed, alpha, tau)
+    if gpu_fields:
+        a = draw_fields_gpu(n_samples, grid, seed, alpha, tau)
+    else:
+        a = draw_fields(n_samples, grid, seed, alpha, tau)
     t0 = time.perf_counter()
     batch = solve_batch(a, f, tol=tol, max_iter=max_iter, preconditioner=preconditioner, form=form)
     elapsed = time.perf_counter() - t0
@@ -71,10 +86,12 @@ def main(argv: list[str] | None = None) -> int:
     p.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--dtype", default="float32", choices=["float32", "float64"])
     p.add_argument("--output", type=Path, default=Path("data/darcy_train.npz"))
+    p.add_argument("--gpu-fields", action="store_true",
+                   help="draw the fields on the GPU too (same distribution, not the reference's random stream)")
     args = p.parse_args(argv)
     try:
         r = generate(args.n_samples, args.grid, args.seed, args.alpha, args.tau, args.f, args.tol, args.max_iter,
-                     args.preconditioner, args.form, args.dtype, args.output)
+                     args.preconditioner, args.form, args.dtype, args.output, gpu_fields=args.gpu_fields)
     except RuntimeError as e:
         print(f"error: {e}", file=sys.stderr)
         return 1

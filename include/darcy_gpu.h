@@ -162,6 +162,16 @@ int dgpu_apply_preconditioner_noalloc(const double* d_a, const double* d_r, int6
  * timed runs). */
 int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes);
 
+/* Random two-phase fields on the GPU for training sets: the reference
+ * generator's construction (python/darcy/fields.py:31-83: spectral amplitudes
+ * tau^(alpha-1) (pi^2 |k|^2 + tau^2)^(-alpha/2), orthonormal inverse DCT,
+ * threshold at zero -> hi / lo) with counter-based noise (Philox-4x32-10,
+ * Box-Muller), so the fields match the host generator in distribution, not
+ * bit for bit. out: count x n x n doubles (n <= 128), on the device when
+ * out_on_device, else host memory; raw != 0 writes the unthresholded field. */
+int dgpu_random_fields(int64_t n, int64_t count, unsigned long long seed, double alpha, double tau, double hi,
+                       double lo, int raw, double* out, int out_on_device, void* stream);
+
 /* ------------------------------------------------------------------------
  * Learned warm start. No counterpart in the reference (which always starts
  * PCG from u0 = 0, solver.hpp:96-102): a 6-layer 3x3 convolutional network
