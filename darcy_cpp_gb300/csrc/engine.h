@@ -142,6 +142,8 @@ void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaSt
 template <class T>
 void launch_visit_pre(const VisitLevel<T>& V, const T* xin, T* xout, T* bc, cudaStream_t s);
 template <class T>
+void launch_visit_mid(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, T* bc, cudaStream_t s);
+template <class T>
 void launch_visit_post(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
                        double* partials, cudaStream_t s);
 template <class T>

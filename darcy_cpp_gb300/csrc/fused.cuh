@@ -263,6 +263,101 @@ __global__ void __launch_bounds__(256) k_visit_pre(VisitLevel<T> V, const T* __r
     if (!waited) pdl_enter();
 }
 
+// The W-cycle's second call of a level follows the first call's
+// post-smoothing directly: post (prolongation, black, red) then pre (red,
+// black, residual, restriction). The two red passes in the middle read the
+// same black values and produce the same result, so one is kept: prolongation
+// + black + red + black + residual/restriction in one kernel, halo 4.
+template <class T, int TH, int TW>
+struct MidSmem {
+    static constexpr int arrays = sizeof(T) == 8 ? 6 : 10;
+    static constexpr size_t bytes = sizeof(T) * arrays * Tile<TH, TW, 4>::S;
+};
+
+template <class T, int TH, int TW>
+__global__ void __launch_bounds__(256) k_visit_mid(VisitLevel<T> V, const T* __restrict__ xin,
+                                                   const T* __restrict__ xc, T* __restrict__ xout,
+                                                   T* __restrict__ bc) {
+    constexpr int R = 4;
+    constexpr bool LO = sizeof(T) == 4;
+    using G = Tile<TH, TW, R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* es = reinterpret_cast<T*>(smem_raw);
+    T* ns = es + G::S;
+    T* ds = ns + G::S;
+    T* is = ds + G::S;
+    T* xs = is + G::S;
+    T* bs = xs + G::S;
+    T* elo = LO ? bs + G::S : nullptr;
+    T* nlo = LO ? elo + G::S : nullptr;
+    T* dlo = LO ? nlo + G::S : nullptr;
+    T* bls = LO ? dlo + G::S : nullptr;
+    const int n = V.n, nc = (n + 1) >> 1;
+    const int tiles_x = (n + TW - 1) / TW, tiles = tiles_x * ((n + TH - 1) / TH);
+    bool waited = false;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int ti0 = (tile / tiles_x) * TH, tj0 = (tile % tiles_x) * TW;
+        stage_coeffs<T, TH, TW, R, true, LO>(V, ti0, tj0, es, ns, ds, is, elo, nlo, dlo);
+        if (!waited) {
+            pdl_enter();
+            waited = true;
+        }
+        stage_vectors<T, TH, TW, R>(V, xin, xc, ti0, tj0, xs, bs, bls);  // x + prolongation
+        __syncthreads();
+        stage_gs<T, TH, TW, R, 1>(n, ti0, tj0, 1, xs, es, ns, is, bs);  // post black, rings <= 3
+        __syncthreads();
+        stage_gs<T, TH, TW, R, 2>(n, ti0, tj0, 0, xs, es, ns, is, bs);  // red (post and pre), rings <= 2
+        __syncthreads();
+        stage_gs<T, TH, TW, R, 3>(n, ti0, tj0, 1, xs, es, ns, is, bs);  // pre black, rings <= 1
+        __syncthreads();
+        for (int q = threadIdx.x; q < (TH / 2) * (TW / 2); q += blockDim.x) {
+            const int ai = q / (TW / 2), aj = q - ai * (TW / 2);
+            const int I = (ti0 >> 1) + ai, J = (tj0 >> 1) + aj;
+            if (I >= nc || J >= nc) continue;
+            if constexpr (sizeof(T) == 8) {
+                T acc = T(0);
+                for (int di = 0; di < 2; ++di) {
+                    if (2 * I + di >= n) break;
+                    for (int dj = 0; dj < 2; ++dj) {
+                        if (2 * J + dj >= n) break;
+                        const int s = (R + 2 * ai + di) * G::SW + (R + 2 * aj + dj);
+                        T v = ds[s] * xs[s];
+                        v -= es[s] * xs[s + 1];
+                        v -= es[s - 1] * xs[s - 1];
+                        v -= ns[s] * xs[s + G::SW];
+                        v -= ns[s - G::SW] * xs[s - G::SW];
+                        acc += bs[s] - v;
+                    }
+                }
+                bc[I * nc + J] = acc;
+            } else {
+                DF acc{0.f, 0.f};
+                for (int di = 0; di < 2; ++di) {
+                    if (2 * I + di >= n) break;
+                    for (int dj = 0; dj < 2; ++dj) {
+                        if (2 * J + dj >= n) break;
+                        const int s = (R + 2 * ai + di) * G::SW + (R + 2 * aj + dj);
+                        df_add(acc, bs[s], bls[s]);
+                        df_axpy(acc, ds[s], dlo[s], xs[s], -1.f);
+                        df_axpy(acc, es[s], elo[s], xs[s + 1], 1.f);
+                        df_axpy(acc, es[s - 1], elo[s - 1], xs[s - 1], 1.f);
+                        df_axpy(acc, ns[s], nlo[s], xs[s + G::SW], 1.f);
+                        df_axpy(acc, ns[s - G::SW], nlo[s - G::SW], xs[s - G::SW], 1.f);
+                    }
+                }
+                bc[I * nc + J] = acc.hi + acc.lo;
+            }
+        }
+        for (int q = threadIdx.x; q < TH * TW; q += blockDim.x) {
+            const int li = q / TW, lj = q - li * TW;
+            const int gi = ti0 + li, gj = tj0 + lj;
+            if (gi < n && gj < n) xout[gi * n + gj] = xs[(R + li) * G::SW + (R + lj)];
+        }
+        __syncthreads();
+    }
+    if (!waited) pdl_enter();
+}
+
 // Prolongation + post-smoothing (1 sweep: black then red). On level 0 (r
 // given) also r . z and beta, like k_gs0_dot.
 template <class T, int TH, int TW>

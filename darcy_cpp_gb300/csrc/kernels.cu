@@ -518,6 +518,15 @@ void launch_visit_pre(const VisitLevel<T>& V, const T* xin, T* xout, T* bc, cuda
                  bc);
 }
 template <class T>
+void launch_visit_mid(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, T* bc, cudaStream_t s) {
+    if (V.n <= 256)
+        launch_k(k_visit_mid<T, 8, 16>, tiles_grid<8, 16>(V.n), 128, MidSmem<T, 8, 16>::bytes, s, V, xin, xc, xout,
+                 bc);
+    else
+        launch_k(k_visit_mid<T, 16, 32>, tiles_grid<16, 32>(V.n), 256, MidSmem<T, 16, 32>::bytes, s, V, xin, xc,
+                 xout, bc);
+}
+template <class T>
 void launch_visit_post(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
                        double* partials, cudaStream_t s) {
     if (V.n <= 256)
@@ -865,6 +874,7 @@ template void launch_cluster_cycle<double>(const ClusterArgs<double>&, int, cuda
     template void launch_dot_rz<T>(const T*, const double*, int64_t, CgState*, double*, cudaStream_t);     \
     template void launch_tail_matvec<T>(const T*, int, const T*, T*, CgState*, cudaStream_t);              \
     template void launch_visit_pre<T>(const VisitLevel<T>&, const T*, T*, T*, cudaStream_t);                 \
+    template void launch_visit_mid<T>(const VisitLevel<T>&, const T*, const T*, T*, T*, cudaStream_t);        \
     template void launch_visit_post<T>(const VisitLevel<T>&, const T*, const T*, T*, const double*,          \
                                        CgState*, double*, cudaStream_t);                                   \
     template void launch_xpby<T>(const T*, double*, int64_t, CgState*, cudaStream_t);                      \

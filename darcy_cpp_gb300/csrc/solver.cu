@@ -446,43 +446,90 @@ VisitLevel<float> visit_level<float>(const GridPlan& P, int l) {
     return VisitLevel<float>{F.n, F.e, F.nf, F.d, F.id, P.elo[l], P.nlo[l], P.dlo[l], F.b, l == 0 ? P.b0lo : nullptr};
 }
 
-// Fused visit (pre_sweeps = post_sweeps = 1): two kernels per level visit,
-// iterates alternating between the level's two buffers. `cur` tracks which
-// buffer holds each level's iterate while the host walks the recursion.
+// Fused visits (pre_sweeps = post_sweeps = 1). The host walks the
+// recursion (multigrid.hpp:97-127) into a list of level operations, merges
+// every post-visit that is directly followed by the next call's pre-visit of
+// the same level into one kernel, then launches the list; iterates alternate
+// between the level's two buffers, `cur` tracking which holds each level's.
+enum VisitKind { kOpPre, kOpPost, kOpMid, kOpTail, kOpCluster };
+struct VisitOp {
+    int kind, l;
+    bool first;
+};
+
+void collect_visits(const GridPlan& P, int l, bool first, std::vector<VisitOp>& ops) {
+    ops.push_back({kOpPre, l, first});
+    if (l + 1 >= P.tail_l0)
+        ops.push_back({kOpTail, l, false});
+    else if (l + 1 == P.cl0)
+        ops.push_back({kOpCluster, l, false});
+    else
+        for (int g = 0; g < P.key.gamma; ++g) collect_visits(P, l + 1, g == 0, ops);
+    ops.push_back({kOpPost, l, false});
+}
+
+std::vector<VisitOp> visit_program(const GridPlan& P) {
+    std::vector<VisitOp> raw, ops;
+    collect_visits(P, 0, true, raw);
+    for (size_t i = 0; i < raw.size(); ++i) {
+        if (raw[i].kind == kOpPost && i + 1 < raw.size() && raw[i + 1].kind == kOpPre && raw[i + 1].l == raw[i].l &&
+            !raw[i + 1].first) {
+            ops.push_back({kOpMid, raw[i].l, false});
+            ++i;
+        } else {
+            ops.push_back(raw[i]);
+        }
+    }
+    return ops;
+}
+
 template <class T>
-void emit_visit_fused(GridPlan& P, int l, bool first, std::vector<int>& cur, cudaStream_t s) {
+void emit_visit_fused(GridPlan& P, std::vector<int>& cur, cudaStream_t s) {
     const auto& lv = levels_of<T>(P);
     const PlanKey& K = P.key;
     auto X = [&](int lvl, int q) { return (T*)(q == 0 ? P.X0[lvl] : P.X1[lvl]); };
-    const VisitLevel<T> V = visit_level<T>(P, l);
-    if (first) {
-        launch_visit_pre<T>(V, nullptr, X(l, 0), lv[l + 1].b, s);
-        cur[l] = 0;
-    } else {
-        launch_visit_pre<T>(V, X(l, cur[l]), X(l, cur[l] ^ 1), lv[l + 1].b, s);
-        cur[l] ^= 1;
+    for (const VisitOp& op : visit_program(P)) {
+        const int l = op.l;
+        const VisitLevel<T> V = visit_level<T>(P, l);
+        switch (op.kind) {
+            case kOpPre:
+                if (op.first) {
+                    launch_visit_pre<T>(V, nullptr, X(l, 0), lv[l + 1].b, s);
+                    cur[l] = 0;
+                } else {
+                    launch_visit_pre<T>(V, X(l, cur[l]), X(l, cur[l] ^ 1), lv[l + 1].b, s);
+                    cur[l] ^= 1;
+                }
+                break;
+            case kOpTail:
+                launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, X(l + 1, 0), P.st, s);
+                cur[l + 1] = 0;
+                break;
+            case kOpCluster: {  // the whole coarse-grid correction in one cluster launch
+                ClusterArgs<T> CA{};
+                CA.nl = P.cl_nl;
+                for (int i = 0; i < P.cl_nl; ++i) CA.lv[i] = visit_level<T>(P, P.cl0 + i);
+                CA.n_tail = P.h[P.tail_l0].n;
+                CA.tail = tail_matrix<T>(P);
+                CA.b_top = lv[l + 1].b;
+                CA.x_top = X(l + 1, 0);
+                CA.gamma = K.gamma;
+                CA.top_calls = K.gamma;
+                launch_cluster_cycle<T>(CA, P.cl_ctas, s);
+                cur[l + 1] = 0;
+                break;
+            }
+            case kOpPost:
+                launch_visit_post<T>(V, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1),
+                                     l == 0 ? P.r : nullptr, P.st, P.partials, s);
+                cur[l] ^= 1;
+                break;
+            case kOpMid:
+                launch_visit_mid<T>(V, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1), lv[l + 1].b, s);
+                cur[l] ^= 1;
+                break;
+        }
     }
-    if (l + 1 >= P.tail_l0) {
-        launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, X(l + 1, 0), P.st, s);
-        cur[l + 1] = 0;
-    } else if (l + 1 == P.cl0) {  // the whole coarse-grid correction in one cluster launch
-        ClusterArgs<T> CA{};
-        CA.nl = P.cl_nl;
-        for (int i = 0; i < P.cl_nl; ++i) CA.lv[i] = visit_level<T>(P, P.cl0 + i);
-        CA.n_tail = P.h[P.tail_l0].n;
-        CA.tail = tail_matrix<T>(P);
-        CA.b_top = lv[l + 1].b;
-        CA.x_top = X(l + 1, 0);
-        CA.gamma = K.gamma;
-        CA.top_calls = K.gamma;
-        launch_cluster_cycle<T>(CA, P.cl_ctas, s);
-        cur[l + 1] = 0;
-    } else {
-        for (int g = 0; g < K.gamma; ++g) emit_visit_fused<T>(P, l + 1, g == 0, cur, s);
-    }
-    launch_visit_post<T>(V, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1), l == 0 ? P.r : nullptr, P.st,
-                         P.partials, s);
-    cur[l] ^= 1;
 }
 
 void emit_setup(GridPlan& P, cudaStream_t s) {
@@ -516,9 +563,9 @@ void emit_precondition(GridPlan& P, cudaStream_t s) {
             // level 0 ends in X1[0] (pre writes X0, post writes X1): z / x0f
             std::vector<int> cur(P.nlev, 0);
             if (P.mixed_mg)
-                emit_visit_fused<float>(P, 0, true, cur, s);
+                emit_visit_fused<float>(P, cur, s);
             else
-                emit_visit_fused<double>(P, 0, true, cur, s);
+                emit_visit_fused<double>(P, cur, s);
         } else if (P.mixed_mg) {
             emit_visit<float>(P, 0, true, s);
         } else {
