@@ -66,6 +66,8 @@ def lib() -> ctypes.CDLL:
                                         _P, ctypes.POINTER(Stats), _P]
         L.dgpu_solve_batch.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
                                        ctypes.POINTER(Options), _P, _P, _P, _P, _P, _P]
+        L.dgpu_solve_batch_device.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int, ctypes.c_int64,
+                                              ctypes.c_int64, ctypes.POINTER(Options), _P, _P, _P, _P, _P, _P, _P, _P]
         L.dgpu_solve_uneven.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.c_double, ctypes.POINTER(Options),
                                         _P, _P, _P, _P, _P, _P]
         L.dgpu_apply_operator.argtypes = [_P, _P, _P, ctypes.c_int64, _P]
@@ -214,6 +216,20 @@ class Context:
         check(lib().dgpu_solve_batch(self.handle, _ptr(a), _ptr(fa), float(f) if fa is None else 0.0, 0, batch, n,
                                      ctypes.byref(opt), None, _ptr(u), _ptr(it), _ptr(res), _ptr(conv), _ptr(lev)))
         return {"u": u, "iterations": it, "residuals": res, "converged": conv.astype(bool), "levels": lev}
+
+    def solve_batch_device(self, d_a: int, batch: int, n: int, d_u: int, stream: int | None = None,
+                           f_scalar: float = 1.0, **kw) -> dict:
+        """Batched solve on device-resident packed arrays (raw device pointers)."""
+        it = np.zeros(batch, dtype=np.int32)
+        res = np.zeros(batch)
+        conv = np.zeros(batch, dtype=np.int32)
+        ms = np.zeros(1)
+        opt = options(**kw)
+        check(lib().dgpu_solve_batch_device(self.handle, ctypes.c_void_p(d_a), None, float(f_scalar), 0, int(batch),
+                                            int(n), ctypes.byref(opt), None, ctypes.c_void_p(d_u), _ptr(it),
+                                            _ptr(res), _ptr(conv), None, _ptr(ms),
+                                            ctypes.c_void_p(stream) if stream else None))
+        return {"iterations": it, "residuals": res, "converged": conv.astype(bool), "device_ms": float(ms[0])}
 
     def solve_uneven(self, fields, f=None, x0=None, f_scalar: float = 1.0, **kw) -> dict:
         """Problems of different sides in one call (dgpu_solve_uneven); f and

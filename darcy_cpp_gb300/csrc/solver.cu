@@ -1333,6 +1333,34 @@ int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double
     });
 }
 
+int dgpu_solve_batch_device(dgpu_context* ctx, const double* d_a, const double* d_f, double f_scalar,
+                            int f_per_sample, int64_t batch, int64_t n, const dgpu_options* opt, const double* d_u0,
+                            double* d_u, int* iterations, double* residuals, int* converged, int* levels,
+                            double* device_ms, void* stream) {
+    return run([&] {
+        if (!ctx) invalid("context must not be NULL");
+        check_options(n, opt);
+        if (batch < 1) invalid("a must have shape (batch, n, n)");
+        if (!d_a || !d_u || !iterations || !residuals || !converged) invalid("buffers must not be NULL");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        cudaStream_t user = (cudaStream_t)stream;
+        if (user) {  // order after the caller's stream
+            CK(cudaEventRecord(ctx->ev0, user));
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev0, 0));
+        }
+        std::vector<int> sides((size_t)batch, (int)n);
+        dgpu_options o = *opt;
+        o.record_history = 0;
+        BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
+        float ms = 0.f;
+        block_solve(ctx, batch, sides, offsets_of(sides), d_a, d_f, f_per_sample ? 0 : 1, f_scalar, d_u0, &o, d_u, bo,
+                    true, &ms);
+        if (device_ms) *device_ms = ms;
+        // block_solve synchronised the context stream: the caller's stream may continue
+    });
+}
+
 int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, const double* a, const double* f,
                       double f_scalar, const dgpu_options* opt, const double* u0, double* u_out, int* iterations,
                       double* residuals, int* converged, int* levels) {

@@ -111,6 +111,15 @@ int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double
                      int64_t batch, int64_t n, const dgpu_options* opt, const double* u0, double* u_out,
                      int* iterations, double* residuals, int* converged, int* levels);
 
+/* Same, on device-resident arrays (d_a, d_f, d_u0, d_u: device pointers,
+ * packed as above); per-sample results in host arrays; device_ms (may be
+ * NULL) receives the device time of the solve. Ordered after `stream` (may be
+ * NULL); returns when the results are written. No reference counterpart. */
+int dgpu_solve_batch_device(dgpu_context* ctx, const double* d_a, const double* d_f, double f_scalar,
+                            int f_per_sample, int64_t batch, int64_t n, const dgpu_options* opt, const double* d_u0,
+                            double* d_u, int* iterations, double* residuals, int* converged, int* levels,
+                            double* device_ms, void* stream);
+
 /* Uneven-size batch (additive extension of solve_batch): problem p has side
  * sides[p] and occupies cells [off_p, off_p + sides[p]^2) of the packed
  * arrays, off_p being the running sum. f/u0 follow the same packing or NULL. */

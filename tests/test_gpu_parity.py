@@ -369,6 +369,23 @@ def test_cluster_coarse_cycle_matches_per_visit_launches(darcy, monkeypatch, n) 
         assert rel_l2(z1, z0) < (1e-12 if form == "fp64" else 1e-5)
 
 
+def test_device_resident_batch_matches_host_batch(darcy) -> None:
+    torch = pytest.importorskip("torch")
+    from darcy_cpp_gb300 import capi
+
+    batch_a = np.stack([two_phase(48, seed=s) for s in range(20)])
+    ctx = capi.Context()
+    d_a = torch.from_numpy(batch_a).cuda()
+    d_u = torch.empty_like(d_a)
+    for form in ("fp64", "mixed"):
+        host = ctx.solve_batch(batch_a, 1.0, form=form)
+        dev = ctx.solve_batch_device(d_a.data_ptr(), 20, 48, d_u.data_ptr(),
+                                     torch.cuda.current_stream().cuda_stream, form=form)
+        assert np.array_equal(host["iterations"], dev["iterations"])
+        assert np.array_equal(host["u"], d_u.cpu().numpy())
+        assert dev["device_ms"] > 0 and dev["converged"].all()
+
+
 def test_uneven_batch_matches_oracle(darcy, orc) -> None:
     sides = [32, 48, 64, 96, 128, 192, 256, 33, 17, 1, 2]
     fields = [two_phase(s, seed=10 + q) for q, s in enumerate(sides)]
