@@ -59,6 +59,13 @@ struct Failure {
 // slower at 1024^2: 44.5 against 38.9 ms, its 4096-column setup and 64 MB
 // products outweighing the launches it saves.)
 constexpr int kTailSide = 32;
+// Uneven batches: problems of at least this side are solved by the grid
+// engine after the block engine has run the rest (one CTA would take seconds
+// on such a grid). Below it the block engine wins even for the largest
+// problems of a batch, since they run beside the small ones: 16384 x 128^2 +
+// 64 x 512^2 took 2.43 s in one block launch and 2.82 s with the 512^2
+// problems routed to the grid engine (FP64).
+constexpr int kGridEngineSide = 768;
 constexpr int kChunk = 8;  // iterations per launch when conditional nodes are unavailable
 
 // Two-pass layout of one device allocation: a pass with base == nullptr only
@@ -874,6 +881,10 @@ void save_tuning(dgpu_context* C) {
 // so that a 64^2 problem keeps levels 32^2 and 16^2 and its 64 x 64 tail on
 // chip with two CTAs per SM.
 size_t smem_budget_for(bool mixed) { return mixed ? 48 * 1024 : 96 * 1024; }
+// A budget large enough for the whole FP32 cycle of a 64^2 problem (every
+// level and the tail on chip, one CTA per SM): then only the FP64 CG vectors
+// and fine-level coefficients live in global memory.
+constexpr size_t kSmemBudgetLarge = 180 * 1024;
 
 // Autotuning key of a batch (loads the tuning file on first use).
 std::string tune_key(dgpu_context* C, int maxside, bool mixed, const dgpu_options* o) {
@@ -1011,7 +1022,8 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         // (1024 threads: one problem per SM, half the resident arenas of 2 x 512,
         // for when the arenas of all resident problems outgrow the L2)
         for (int threads : {128, 256, 512, 1024})
-            for (size_t smem : {(size_t)0, smem_budget_for(mixed)}) {
+            for (size_t smem : {(size_t)0, smem_budget_for(mixed), kSmemBudgetLarge}) {
+                if (smem == kSmemBudgetLarge && (!mixed || threads < 512)) continue;
                 const BlockConfig c{threads, smem};
                 launch(c, sample);  // warm (allocations, clocks)
                 CK(cudaEventRecord(C->ev0, s));
@@ -1377,8 +1389,46 @@ int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, co
         CK(cudaSetDevice(ctx->device));
         dgpu_options o = *opt;
         o.record_history = 0;
-        BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
-        block_solve(ctx, count, sv, offsets_of(sv), a, f, 0, f_scalar, u0, &o, u_out, bo, false, nullptr);
+        // Problems of side >= kGridEngineSide go to the grid engine, one
+        // graph-launched solve each, after the block engine has taken the
+        // rest: on one CTA such a problem would outlast the whole batch.
+        const std::vector<int64_t> off = offsets_of(sv);
+        std::vector<int64_t> small, big;
+        for (int64_t q = 0; q < count; ++q) (sv[q] >= kGridEngineSide ? big : small).push_back(q);
+        if (big.empty()) {
+            BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
+            block_solve(ctx, count, sv, off, a, f, 0, f_scalar, u0, &o, u_out, bo, false, nullptr);
+            return;
+        }
+        if (!small.empty()) {
+            const size_t ns = small.size();
+            std::vector<int> ss(ns), it(ns), cv(ns), lv(ns);
+            std::vector<int64_t> so(ns);
+            std::vector<double> rs(ns);
+            for (size_t k = 0; k < ns; ++k) {
+                ss[k] = sv[small[k]];
+                so[k] = off[small[k]];
+            }
+            BatchOut bo{it.data(), rs.data(), cv.data(), lv.data(), nullptr, nullptr};
+            block_solve(ctx, (int64_t)ns, ss, so, a, f, 0, f_scalar, u0, &o, u_out, bo, false, nullptr);
+            for (size_t k = 0; k < ns; ++k) {
+                iterations[small[k]] = it[k];
+                residuals[small[k]] = rs[k];
+                converged[small[k]] = cv[k];
+                if (levels) levels[small[k]] = lv[k];
+            }
+        }
+        // (the block engine's copy-out covers the cells up to its last
+        // problem; the large problems' cells are written after it)
+        for (int64_t q : big) {
+            dgpu_stats st{};
+            grid_solve(ctx, a + off[q], f ? f + off[q] : nullptr, f_scalar, sv[q], &o, u0 ? u0 + off[q] : nullptr,
+                       u_out + off[q], nullptr, &st, false, nullptr);
+            iterations[q] = st.iterations;
+            residuals[q] = st.residual;
+            converged[q] = st.converged;
+            if (levels) levels[q] = st.levels;
+        }
     });
 }
 

@@ -386,6 +386,19 @@ def test_device_resident_batch_matches_host_batch(darcy) -> None:
         assert dev["device_ms"] > 0 and dev["converged"].all()
 
 
+def test_uneven_batch_routes_large_problems_to_the_grid_engine(darcy) -> None:
+    sides = [32, 800, 48, 20]
+    fields = [two_phase(s, seed=70 + q) for q, s in enumerate(sides)]
+    for form in ("fp64", "mixed"):
+        out = darcy.solve_batch_uneven(fields, tol=1e-10, form=form)
+        assert out.all_converged
+        for q, a in enumerate(fields):
+            single = darcy.solve(a, tol=1e-10, form=form)
+            assert out.levels[q] == single.levels
+            assert abs(out.iterations[q] - single.iterations) <= 1
+            assert rel_l2(out.u[q], single.u) < 1e-9
+
+
 def test_uneven_batch_matches_oracle(darcy, orc) -> None:
     sides = [32, 48, 64, 96, 128, 192, 256, 33, 17, 1, 2]
     fields = [two_phase(s, seed=10 + q) for q, s in enumerate(sides)]
