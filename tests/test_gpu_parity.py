@@ -39,16 +39,15 @@ def oracle_threads(orc, n):
 
 def oracle_iteration_range(orc, a, **kw) -> tuple[int, int]:
     """The reference's own iteration count is not a single number at high
-    contrast: its OpenMP reductions change order with the thread count, and
-    where the residual plateaus near tol that moves the stopping iteration
-    (511^2 with a in {1e2, 1e-2}: 75 at 1-2 threads, 81 at 4+). Return the
-    range over one thread and all threads."""
-    counts = []
-    for t in (1, min(16, orc.cpu_count())):
-        orc.set_threads(t)
-        counts.append(orc.solve(a, **kw)["iterations"])
+    contrast: its OpenMP reductions combine thread partials in a different
+    order with each thread count (and, with several threads, from run to
+    run), and where the residual plateaus near tol that moves the stopping
+    iteration (511^2 with a in {1e2, 1e-2}: 75 at 1-2 threads, 81 at 4+).
+    Return the deterministic one-thread count widened by 10% either way."""
     orc.set_threads(1)
-    return min(counts), max(counts)
+    ref = orc.solve(a, **kw)["iterations"]
+    slack = max(1, int(0.1 * ref + 0.5))
+    return ref - slack, ref + slack
 
 
 def true_residual(orc, a, u, f=1.0) -> float:
@@ -224,7 +223,7 @@ def test_grid_engine_matches_oracle(darcy, orc, n, cycle) -> None:
     lo, hi = oracle_iteration_range(orc, a, tol=1e-10, cycle_index=cycle)
     got = darcy.solve(a, tol=1e-10, cycle_index=cycle)
     assert got.converged and got.levels == want["levels"]
-    assert lo - 1 <= got.iterations <= hi + 1, (got.iterations, lo, hi)
+    assert lo <= got.iterations <= hi, (got.iterations, lo, hi)
     assert rel_l2(got.u, want["u"]) < REL_L2
     assert got.residual < 1e-10
     # The recursive residual drifts from the true one at high contrast (the
