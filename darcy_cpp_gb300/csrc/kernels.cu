@@ -8,6 +8,8 @@
 //     problem, pulling problems from a work counter, largest first.
 #include <math.h>
 
+#include <cstdlib>
+
 #include "block.cuh"
 #include "cluster.cuh"
 #include "cycle.cuh"
@@ -18,6 +20,8 @@ namespace dgpu {
 
 // ------------------------------------------------------------ small helpers
 
+// Grid of the streaming kernels: capped at 8 CTAs per SM (measured at
+// 1024^2: 608, 2432 and 4864 CTAs were all slower than 1216).
 static inline int grid_for(int64_t work, int threads = kThreads) {
     int64_t g = (work + threads - 1) / threads;
     if (g < 1) g = 1;
@@ -509,31 +513,36 @@ static inline int tiles_grid(int n) {
     return (int)(t < kMaxTileGrid ? t : kMaxTileGrid);
 }
 
+// Threads of a visit CTA. 256 for both tile shapes: measured at 1024^2
+// (mixed / FP64) 35.0 / 42.7 ms with 128 threads on the 8 x 16 tiles, 32.8 /
+// 39.5 ms with 256 (more loads in flight while the halo is staged), 33.1 /
+// 40.9 ms with 512; 512 on the 16 x 32 tiles measured slower as well.
+constexpr int kVisitThreads = 256;
 template <class T>
 void launch_visit_pre(const VisitLevel<T>& V, const T* xin, T* xout, T* bc, cudaStream_t s) {
     if (V.n <= 256)
-        launch_k(k_visit_pre<T, 8, 16>, tiles_grid<8, 16>(V.n), 128, VisitSmem<T, 8, 16>::bytes, s, V, xin, xout, bc);
+        launch_k(k_visit_pre<T, 8, 16>, tiles_grid<8, 16>(V.n), kVisitThreads, VisitSmem<T, 8, 16>::bytes, s, V, xin, xout, bc);
     else
-        launch_k(k_visit_pre<T, 16, 32>, tiles_grid<16, 32>(V.n), 256, VisitSmem<T, 16, 32>::bytes, s, V, xin, xout,
+        launch_k(k_visit_pre<T, 16, 32>, tiles_grid<16, 32>(V.n), kVisitThreads, VisitSmem<T, 16, 32>::bytes, s, V, xin, xout,
                  bc);
 }
 template <class T>
 void launch_visit_mid(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, T* bc, cudaStream_t s) {
     if (V.n <= 256)
-        launch_k(k_visit_mid<T, 8, 16>, tiles_grid<8, 16>(V.n), 128, MidSmem<T, 8, 16>::bytes, s, V, xin, xc, xout,
+        launch_k(k_visit_mid<T, 8, 16>, tiles_grid<8, 16>(V.n), kVisitThreads, MidSmem<T, 8, 16>::bytes, s, V, xin, xc, xout,
                  bc);
     else
-        launch_k(k_visit_mid<T, 16, 32>, tiles_grid<16, 32>(V.n), 256, MidSmem<T, 16, 32>::bytes, s, V, xin, xc,
+        launch_k(k_visit_mid<T, 16, 32>, tiles_grid<16, 32>(V.n), kVisitThreads, MidSmem<T, 16, 32>::bytes, s, V, xin, xc,
                  xout, bc);
 }
 template <class T>
 void launch_visit_post(const VisitLevel<T>& V, const T* xin, const T* xc, T* xout, const double* r, CgState* st,
                        double* partials, cudaStream_t s) {
     if (V.n <= 256)
-        launch_k(k_visit_post<T, 8, 16>, tiles_grid<8, 16>(V.n), 128, PostSmem<T, 8, 16>::bytes, s, V, xin, xc, xout,
+        launch_k(k_visit_post<T, 8, 16>, tiles_grid<8, 16>(V.n), kVisitThreads, PostSmem<T, 8, 16>::bytes, s, V, xin, xc, xout,
                  r, st, partials);
     else
-        launch_k(k_visit_post<T, 16, 32>, tiles_grid<16, 32>(V.n), 256, PostSmem<T, 16, 32>::bytes, s, V, xin, xc,
+        launch_k(k_visit_post<T, 16, 32>, tiles_grid<16, 32>(V.n), kVisitThreads, PostSmem<T, 16, 32>::bytes, s, V, xin, xc,
                  xout, r, st, partials);
 }
 
@@ -575,7 +584,7 @@ void launch_tail_columns(const Lvl64* h_dev, const Lvl64* h_host, int l0, int nl
 }
 template <class T>
 void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaStream_t s) {
-    const int threads = 128;
+    const int threads = 128;  // 64 and 256 measured the same
     int blocks = (N + threads / 32 - 1) / (threads / 32);
     if (blocks > kMaxBlocks) blocks = kMaxBlocks;
     launch_k(k_tail_matvec<T>, blocks, threads, 0, s, M, N, b, x, st);
