@@ -50,7 +50,8 @@ template <class T>
 struct BlockViews {
     Lvl64 h[kMaxLevels];        // FP64 hierarchy
     Lvl<T> lv[kMaxLevels];      // the cycle's levels
-    Lvl<double> lm[kMaxLevels]; // tail construction: FP64 levels with N right-hand sides
+    Lvl<T> lm[kMaxLevels];      // tail construction: the tail levels with N right-hand sides, in the
+                                // cycle's precision (FP32 copies of the coefficients for the mixed form)
     double* cg[5];              // b, r, p, Ap, z
     T* tail;                    // dense tail operator (ntail x ntail), or null
     int nlev, tl, ntail;
@@ -163,17 +164,22 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
     if (tl) {  // tail construction scratch: every tail level with ntail right-hand sides
         for (int l = tl; l < nlev; ++l) {
             const size_t m = (size_t)sides[l] * sides[l];
-            Lvl<double> M{};
+            Lvl<T> M{};
             M.n = sides[l];
-            M.x = (double*)gtake(8 * m * ntail);
-            M.b = (double*)gtake(8 * m * ntail);
-            if (v) {
-                M.e = v->h[l].e;
-                M.nf = v->h[l].nf;
-                M.d = v->h[l].d;
-                M.id = v->h[l].id;
-                v->lm[l] = M;
+            M.x = (T*)gtake(sizeof(T) * m * ntail);
+            M.b = (T*)gtake(sizeof(T) * m * ntail);
+            if (fp32) {
+                M.e = (const T*)gtake(sizeof(T) * m);
+                M.nf = (const T*)gtake(sizeof(T) * m);
+                M.d = (const T*)gtake(sizeof(T) * m);
+                M.id = (const T*)gtake(sizeof(T) * m);
+            } else if (v) {
+                M.e = (const T*)v->h[l].e;
+                M.nf = (const T*)v->h[l].nf;
+                M.d = (const T*)v->h[l].d;
+                M.id = (const T*)v->h[l].id;
             }
+            if (v) v->lm[l] = M;
         }
     }
     return BlockLayout{goff, soff, nlev, ls};
@@ -241,21 +247,22 @@ __device__ double block_precondition(const BatchArgs& A, const BlockViews<T>& V,
 }
 
 // The dense tail of one problem: column j = the tail map applied to e_j, all
-// columns at once in FP64 on the FP64 hierarchy, then stored (rounded for the
-// FP32 cycle) row-major.
+// columns at once, in the cycle's precision (the FP32 smoothing of the mixed
+// form, with the exact 1 x 1 coarsest solve in FP64), stored row-major.
+// Building it in FP64 cost the mixed form about a third of its FP64 work.
 template <class T>
 __device__ void block_build_tail(const BatchArgs& A, const BlockViews<T>& V) {
     const int tl = V.tl, N = V.ntail;
-    const Lvl<double>& L = V.lm[tl];
+    const Lvl<T>& L = V.lm[tl];
     for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
         const int j = t / N, k = t - j * N;  // right-hand side j, cell k
-        L.b[t] = (k == j) ? 1.0 : 0.0;
+        L.b[t] = (k == j) ? T(1) : T(0);
     }
     __syncthreads();
-    block_cycle_m<double>(V.lm, tl, V.nlev, A.pre, A.post, A.gamma, A.gamma, N);
+    block_cycle_m<T>(V.lm, tl, V.nlev, A.pre, A.post, A.gamma, A.gamma, N, V.h[V.nlev - 1].id);
     for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
         const int j = t / N, k = t - j * N;
-        V.tail[k * N + j] = (T)L.x[t];
+        V.tail[k * N + j] = L.x[t];
     }
     __syncthreads();
 }
@@ -275,6 +282,7 @@ __device__ unsigned long long block_setup(const BatchArgs& A, const double* a, c
     }
     if (A.pc == kPcMultigrid) {
         for (int l = 0; l < V.nlev; ++l) block_copy_coeffs<T>(V.h[l], V.lv[l]);
+        for (int l = V.tl ? V.tl : V.nlev; l < V.nlev; ++l) block_copy_coeffs<T>(V.h[l], V.lm[l]);
         __syncthreads();
         if (V.tl && *s_bad == ~0ull) block_build_tail<T>(A, V);
     }

@@ -190,9 +190,11 @@ __device__ __forceinline__ void prolong_gs1_m(const Lvl<T> L, const T* xc, int n
     }
 }
 
+// id64: the FP64 reciprocal diagonal of the coarsest level (its 1 x 1 solve
+// stays FP64 when the cycle is FP32), or null.
 template <class T>
 __device__ void block_cycle_m(const Lvl<T>* lv, int l0, int nlev, int pre, int post, int gamma, int top_calls,
-                              int nrhs) {
+                              int nrhs, const double* id64 = nullptr) {
     int calls[kMaxLevels];
     unsigned zero_mask = 1u << l0;
     int l = l0;
@@ -217,7 +219,8 @@ __device__ void block_cycle_m(const Lvl<T>* lv, int l0, int nlev, int pre, int p
             const Lvl<T>& A = lv[l];
             const bool zero = (zero_mask >> l) & 1u;
             if (A.n == 1) {
-                for (int rr = threadIdx.x; rr < nrhs; rr += blockDim.x) A.x[rr] = A.b[rr] * A.id[0];
+                for (int rr = threadIdx.x; rr < nrhs; rr += blockDim.x)
+                    A.x[rr] = id64 ? (T)((double)A.b[rr] * id64[0]) : A.b[rr] * A.id[0];
                 __syncthreads();
             } else {
                 for (int s = 0; s < 8; ++s) {
