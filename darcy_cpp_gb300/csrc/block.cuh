@@ -217,15 +217,17 @@ __device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* 
 // into the level-0 right-hand side and the FP32 iterate widened into z.
 template <class T>
 __device__ double block_precondition(const BatchArgs& A, const BlockViews<T>& V, const double* r, double* z,
-                                     double* red) {
+                                     double* red, bool b_ready = false) {
     const int n = V.h[0].n;
     const int64_t m = (int64_t)n * n;
     double acc = 0.0;
     if (A.pc == kPcMultigrid) {
         const double* id64 = V.h[V.nlev - 1].id;  // FP64 exact coarsest solve (no-tail hierarchies)
         if (sizeof(T) == 4) {
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) V.lv[0].b[k] = (T)r[k];
-            __syncthreads();
+            if (!b_ready) {  // (the CG update usually wrote the rounded r already)
+                for (int64_t k = threadIdx.x; k < m; k += blockDim.x) V.lv[0].b[k] = (T)r[k];
+                __syncthreads();
+            }
             block_cycle<T>(V.lv, 0, V.nlev, A.pre, A.post, A.gamma, 1, id64, V.tail, V.tl);
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
                 const double zk = (double)V.lv[0].x[k];

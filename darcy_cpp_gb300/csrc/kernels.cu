@@ -654,7 +654,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             A.converged[pid] = 0;
             A.residual[pid] = 0.0;
             A.levels[pid] = 1;
-            A.true_residual[pid] = 0.0;
+            if (A.true_residual) A.true_residual[pid] = 0.0;
         }
         return;
     }
@@ -689,7 +689,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             A.converged[pid] = 1;
             A.residual[pid] = 0.0;
             A.levels[pid] = 1;
-            A.true_residual[pid] = 0.0;
+            if (A.true_residual) A.true_residual[pid] = 0.0;
         }
         return;
     }
@@ -725,11 +725,15 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             }
             const double alpha = rz / pap;
             double rr = 0.0, rzo = 0.0;
+            // the FP32 cycle's input (r rounded) is written here, in the same pass
+            const bool round_b = sizeof(T) == 4 && A.pc == kPcMultigrid;
+            T* b32 = V.lv[0].b;
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
                 u[k] += alpha * p[k];
                 const double rk = r[k] - alpha * ap[k];
                 r[k] = rk;
                 rr += rk * rk;
+                if (round_b) b32[k] = (T)rk;
                 if (flexible) rzo += rk * z[k];  // z still holds the previous direction's z
             }
             residual = sqrt(block_sum(rr, red)) / bnorm;
@@ -740,7 +744,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
                 converged = 1;
                 break;
             }
-            const double rz_new = block_precondition<T>(A, V, r, z, red);
+            const double rz_new = block_precondition<T>(A, V, r, z, red, round_b);
             const double beta = (rz_new - rzo) / rz;
             rz = rz_new;
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k] + beta * p[k];
@@ -748,15 +752,19 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         }
     }
 
-    // Honest residual: ||b - A u|| / ||b|| from scratch.
-    double tr = 0.0;
+    // Honest residual ||b - A u|| / ||b|| from scratch, when the caller asked
+    // for it (one more FP64 operator pass per problem).
+    double true_res = residual;
     __syncthreads();
-    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
-        const double rk = b[k] - apply_cell(h[0], u, i, j);
-        tr += rk * rk;
+    if (A.true_residual) {
+        double tr = 0.0;
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+            const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
+            const double rk = b[k] - apply_cell(h[0], u, i, j);
+            tr += rk * rk;
+        }
+        true_res = sqrt(block_sum(tr, red)) / bnorm;
     }
-    const double true_res = sqrt(block_sum(tr, red)) / bnorm;
     if (A.u_host)
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) A.u_host[off + k] = u[k];
     if (threadIdx.x == 0) {
@@ -765,7 +773,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         A.converged[pid] = converged;
         A.residual[pid] = residual;
         A.levels[pid] = A.pc == kPcMultigrid ? nlev : 1;
-        A.true_residual[pid] = true_res;
+        if (A.true_residual) A.true_residual[pid] = true_res;
     }
 }
 

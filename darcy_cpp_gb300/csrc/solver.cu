@@ -932,7 +932,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     A.residual = C->bres.ensure(count);
     A.converged = C->bconv.ensure(count);
     A.levels = C->blev.ensure(count);
-    A.true_residual = C->btrue.ensure(count);
+    A.true_residual = out.true_residual ? C->btrue.ensure(count) : nullptr;
     A.bad = C->bbad.ensure(count);
     A.work = C->bwork.ensure(2);
     A.history = (o->record_history && count == 1) ? C->bhist.ensure((size_t)o->max_iter + 1) : nullptr;
