@@ -68,6 +68,8 @@ def lib() -> ctypes.CDLL:
                                        ctypes.POINTER(Options), _P, _P, _P, _P, _P, _P]
         L.dgpu_solve_batch_device.argtypes = [_P, _P, _P, ctypes.c_double, ctypes.c_int, ctypes.c_int64,
                                               ctypes.c_int64, ctypes.POINTER(Options), _P, _P, _P, _P, _P, _P, _P, _P]
+        L.dgpu_last_launches.argtypes = [_P]
+        L.dgpu_last_launches.restype = ctypes.c_int64
         L.dgpu_solve_uneven.argtypes = [_P, ctypes.c_int64, _P, _P, _P, ctypes.c_double, ctypes.POINTER(Options),
                                         _P, _P, _P, _P, _P, _P]
         L.dgpu_apply_operator.argtypes = [_P, _P, _P, ctypes.c_int64, _P]
@@ -229,7 +231,8 @@ class Context:
                                             int(n), ctypes.byref(opt), None, ctypes.c_void_p(d_u), _ptr(it),
                                             _ptr(res), _ptr(conv), None, _ptr(ms),
                                             ctypes.c_void_p(stream) if stream else None))
-        return {"iterations": it, "residuals": res, "converged": conv.astype(bool), "device_ms": float(ms[0])}
+        return {"iterations": it, "residuals": res, "converged": conv.astype(bool), "device_ms": float(ms[0]),
+                "kernel_launches": int(lib().dgpu_last_launches(self.handle))}
 
     def solve_uneven(self, fields, f=None, x0=None, f_scalar: float = 1.0, **kw) -> dict:
         """Problems of different sides in one call (dgpu_solve_uneven); f and

@@ -20,6 +20,8 @@
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <atomic>
+#include <thread>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -59,13 +61,22 @@ struct Failure {
 // slower at 1024^2: 44.5 against 38.9 ms, its 4096-column setup and 64 MB
 // products outweighing the launches it saves.)
 constexpr int kTailSide = 32;
-// Uneven batches: problems of at least this side are solved by the grid
-// engine after the block engine has run the rest (one CTA would take seconds
-// on such a grid). Below it the block engine wins even for the largest
-// problems of a batch, since they run beside the small ones: 16384 x 128^2 +
-// 64 x 512^2 took 2.43 s in one block launch and 2.82 s with the 512^2
-// problems routed to the grid engine (FP64).
+// Batch routing between the engines. A problem of side >= kGridEngineSide
+// goes to the grid engine, several such solves at once on their own streams
+// (grid_solve_many), after the block engine has run the rest. A problem of
+// side >= kGridEngineMinSide goes there too when it is more work than one
+// CTA's share of the batch (its cells > all cells / (2 x SMs)): on one CTA it
+// would outlast the rest, while beside many smaller problems it is hidden.
+// Measured on GB300 (device-resident, FP64 / mixed): 64 x 384^2 at contrast
+// 1e4, 481 / 553 ms on the block engine, 199 / 177 ms on the grid engine;
+// 64 x 512^2, 1097 / 1188 against 373 / 307 ms; 128 x 256^2 at contrast 4,
+// 71 / 55 against 182 / 140 ms (hence the lower bound); 16384 x 128^2 +
+// 64 x 512^2, 1423 / 1252 ms with the 512^2 problems in the block launch,
+// 1659 / 1344 ms with them routed (hence the share rule).
 constexpr int kGridEngineSide = 768;
+constexpr int kGridEngineMinSide = 384;
+// Concurrent grid-engine solves of a batch of large problems.
+constexpr int kGridSlots = 4;
 constexpr int kChunk = 8;  // iterations per launch when conditional nodes are unavailable
 
 // Two-pass layout of one device allocation: a pass with base == nullptr only
@@ -154,9 +165,10 @@ std::vector<int> level_sides(int n) {
 
 struct PlanKey {
     int n, form, pc, pre, post, gamma, has_f, has_u0;
+    int slot = 0;  // instance of concurrent solves (grid_solve_many), 0 otherwise
     bool operator<(const PlanKey& o) const {
-        return std::tie(n, form, pc, pre, post, gamma, has_f, has_u0) <
-               std::tie(o.n, o.form, o.pc, o.pre, o.post, o.gamma, o.has_f, o.has_u0);
+        return std::tie(n, form, pc, pre, post, gamma, has_f, has_u0, slot) <
+               std::tie(o.n, o.form, o.pc, o.pre, o.post, o.gamma, o.has_f, o.has_u0, o.slot);
     }
 };
 
@@ -239,6 +251,10 @@ struct dgpu_context {
     std::map<std::string, BlockConfigPOD> tuned;
     int last_block_threads = 0;
     size_t last_block_smem = 0;
+    // concurrent grid-engine solves: one stream, event pair and plan per slot
+    std::vector<cudaStream_t> slot_streams;
+    std::vector<cudaEvent_t> slot_events;
+    std::map<PlanKey, std::unique_ptr<GridPlan>> slot_plans;
 };
 
 namespace {
@@ -714,36 +730,25 @@ void check_options(int64_t n, const dgpu_options* o) {
 
 // ----------------------------------------------------------------- grid solve
 
-void grid_solve(dgpu_context* C, const double* a, const double* f, double fscalar, int64_t n,
-                const dgpu_options* o, const double* u0, double* u_out, double* history_out, dgpu_stats* stats,
-                bool device_ptrs, cudaStream_t user_stream) {
-    PlanKey K{(int)n, o->form, o->preconditioner, o->pre_sweeps, o->post_sweeps, o->cycle_index, f != nullptr,
-              u0 != nullptr};
-    GridPlan& P = get_plan(C, K);
-    cudaStream_t s = C->stream;
+// One solve through plan P on stream s (events e0/e1 bracket it for
+// device_ms): H2D copies, one graph launch, D2H copies, synchronise.
+void grid_run(GridPlan& P, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, const double* a, const double* f,
+              double fscalar, const dgpu_options* o, const double* u0, double* u_out, double* hist,
+              dgpu_stats* stats, bool device_ptrs) {
     const size_t bytes = sizeof(double) * (size_t)P.m;
     const cudaMemcpyKind in = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const cudaMemcpyKind out = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (user_stream) {
-        cudaEvent_t e;
-        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        CK(cudaEventRecord(e, user_stream));
-        CK(cudaStreamWaitEvent(s, e, 0));
-        cudaEventDestroy(e);
-    }
-    double* hist = nullptr;
-    if (o->record_history) hist = P.history.ensure((size_t)o->max_iter + 1);
     CgState& hs = *P.st_host.p;
     std::memset(&hs, 0, sizeof hs);
     hs.tol = o->tol;
     hs.fscalar = fscalar;
     hs.max_iter = o->max_iter;
-    hs.record_history = o->record_history ? 1 : 0;
+    hs.record_history = hist ? 1 : 0;
     hs.history = hist;
     hs.use_cond = P.cond ? 1 : 0;
     hs.cond = P.handle;
     hs.bad = ~0ull;
-    CK(cudaEventRecord(C->ev0, s));
+    CK(cudaEventRecord(e0, s));
     CK(cudaMemcpyAsync(P.a, a, bytes, in, s));
     if (f) CK(cudaMemcpyAsync(P.f, f, bytes, in, s));
     if (u0) CK(cudaMemcpyAsync(P.u0, u0, bytes, in, s));
@@ -762,25 +767,18 @@ void grid_solve(dgpu_context* C, const double* a, const double* f, double fscala
     }
     CK(cudaMemcpyAsync(u_out, P.u, bytes, out, s));
     CK(cudaMemcpyAsync(&hs, P.st, sizeof hs, cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(C->ev1, s));
-    if (user_stream) {
-        cudaEvent_t e;
-        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        CK(cudaEventRecord(e, s));
-        CK(cudaStreamWaitEvent(user_stream, e, 0));
-        cudaEventDestroy(e);
-    }
+    CK(cudaEventRecord(e1, s));
     CK(cudaStreamSynchronize(s));
     if (hs.bad != ~0ull) bad_permeability(hs.bad);
     float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, C->ev0, C->ev1));
+    CK(cudaEventElapsedTime(&ms, e0, e1));
     const bool f_zero = hs.bnorm == 0.0;
     if (stats) {
         stats->iterations = hs.it;
         stats->residual = hs.residual;
         stats->converged = hs.converged;
         stats->levels = (o->preconditioner == kPcMultigrid && !f_zero) ? P.nlev : 1;
-        stats->history_len = o->record_history ? hs.it + 1 : 0;
+        stats->history_len = hist ? hs.it + 1 : 0;
         stats->true_residual = hs.true_residual;
         stats->device_ms = ms;
         // the loop body runs once per iteration, and once more (all early
@@ -788,8 +786,148 @@ void grid_solve(dgpu_context* C, const double* a, const double* f, double fscala
         const int64_t bodies = std::max(hs.it, 1);
         stats->kernel_launches = (int64_t)P.nodes_pro + bodies * (int64_t)P.nodes_body + (int64_t)P.nodes_epi;
     }
-    if (history_out && o->record_history)
-        CK(cudaMemcpy(history_out, hist, sizeof(double) * ((size_t)hs.it + 1), cudaMemcpyDeviceToHost));
+}
+
+void grid_solve(dgpu_context* C, const double* a, const double* f, double fscalar, int64_t n,
+                const dgpu_options* o, const double* u0, double* u_out, double* history_out, dgpu_stats* stats,
+                bool device_ptrs, cudaStream_t user_stream) {
+    PlanKey K{(int)n, o->form, o->preconditioner, o->pre_sweeps, o->post_sweeps, o->cycle_index, f != nullptr,
+              u0 != nullptr};
+    GridPlan& P = get_plan(C, K);
+    cudaStream_t s = C->stream;
+    if (user_stream) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaEventRecord(e, user_stream));
+        CK(cudaStreamWaitEvent(s, e, 0));
+        cudaEventDestroy(e);
+    }
+    double* hist = nullptr;
+    if (o->record_history) hist = P.history.ensure((size_t)o->max_iter + 1);
+    dgpu_stats st{};
+    // (grid_run synchronises s before returning, so the caller's stream is
+    // ordered after the solve without a further event)
+    grid_run(P, s, C->ev0, C->ev1, a, f, fscalar, o, u0, u_out, hist, &st, device_ptrs);
+    if (stats) *stats = st;
+    C->last_launches = st.kernel_launches;
+    if (history_out && hist)
+        CK(cudaMemcpy(history_out, hist, sizeof(double) * ((size_t)st.iterations + 1), cudaMemcpyDeviceToHost));
+}
+
+// Whether a batched problem of side n goes to the grid engine, in a batch of
+// total_cells cells. DARCY_GPU_GRID_SIDE=s overrides: side >= s, nothing else.
+bool route_to_grid(const dgpu_context* C, int64_t n, int64_t total_cells) {
+    const char* e = std::getenv("DARCY_GPU_GRID_SIDE");
+    const int v = e ? std::atoi(e) : 0;
+    if (v >= 1) return n >= v;
+    if (n >= kGridEngineSide) return true;
+    return n >= kGridEngineMinSide && n * n > total_cells / (2 * (int64_t)std::max(C->sms, 1));
+}
+
+// Concurrent slots for grid_solve_many (DARCY_GPU_SLOTS overrides, 1..16).
+int grid_slots() {
+    const char* e = std::getenv("DARCY_GPU_SLOTS");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= 16 ? v : kGridSlots;
+}
+
+// Many grid-engine solves of one side at once. A single large solve leaves
+// most SMs idle in its coarse levels (the W-cycle's many small dependent
+// launches); solves on separate streams fill them. Each slot owns a plan
+// (buffers + graph), a stream and a host thread that pulls problems from a
+// shared counter, so pageable host arrays work and slots never wait on one
+// another's copies. Problems are taken in `order`; problem q reads
+// a + off[q] (u0 at the same offset when given; f too unless f_shared) and
+// writes u_out + off[q].
+// Returns the device time from the first to the last slot's work (ms).
+float grid_solve_many(dgpu_context* C, int side, const std::vector<int64_t>& order, const std::vector<int64_t>& off,
+                      const double* a, const double* f, bool f_shared, double fscalar, const dgpu_options* o,
+                      const double* u0,
+                      double* u_out, int* iterations, double* residuals, int* converged, int* levels,
+                      bool device_ptrs) {
+    const int S = (int)std::min<int64_t>((int64_t)order.size(), grid_slots());
+    while ((int)C->slot_streams.size() < S) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        C->slot_streams.push_back(st);
+        for (int k = 0; k < 2; ++k) {
+            cudaEvent_t ev;
+            CK(cudaEventCreate(&ev));
+            C->slot_events.push_back(ev);
+        }
+    }
+    // slot plans of one problem family at a time (they hold O(n^2) memory each)
+    PlanKey K{side, o->form, o->preconditioner, o->pre_sweeps, o->post_sweeps, o->cycle_index, f != nullptr,
+              u0 != nullptr};
+    if (!C->slot_plans.empty()) {
+        PlanKey k0 = C->slot_plans.begin()->first;
+        k0.slot = 0;
+        if (k0 < K || K < k0) C->slot_plans.clear();
+    }
+    std::vector<GridPlan*> plans((size_t)S);
+    for (int q = 0; q < S; ++q) {
+        K.slot = q;
+        auto it = C->slot_plans.find(K);
+        if (it == C->slot_plans.end()) {
+            auto P = std::make_unique<GridPlan>();
+            P->key = K;
+            alloc_plan(C, *P);
+            build_graphs(C, *P);
+            it = C->slot_plans.emplace(K, std::move(P)).first;
+        }
+        plans[(size_t)q] = it->second.get();
+    }
+    // every slot starts after the work already on the context stream
+    CK(cudaEventRecord(C->ev0, C->stream));
+    for (int q = 0; q < S; ++q) CK(cudaStreamWaitEvent(C->slot_streams[(size_t)q], C->ev0, 0));
+    std::atomic<int64_t> next{0};
+    std::atomic<bool> stop{false};
+    std::vector<Failure> fails((size_t)S, Failure{DGPU_OK, ""});
+    std::vector<int64_t> launches((size_t)S, 0);
+    auto worker = [&](int q) {
+        try {
+            CK(cudaSetDevice(C->device));
+            cudaStream_t s = C->slot_streams[(size_t)q];
+            for (;;) {
+                const int64_t k = next.fetch_add(1);
+                if (k >= (int64_t)order.size() || stop.load()) break;
+                const int64_t p = order[(size_t)k];
+                const int64_t at = off[(size_t)p];
+                dgpu_stats st{};
+                grid_run(*plans[(size_t)q], s, C->slot_events[2 * (size_t)q], C->slot_events[2 * (size_t)q + 1],
+                         a + at, f ? (f_shared ? f : f + at) : nullptr, fscalar, o, u0 ? u0 + at : nullptr, u_out + at, nullptr, &st,
+                         device_ptrs);
+                iterations[p] = st.iterations;
+                residuals[p] = st.residual;
+                converged[p] = st.converged;
+                if (levels) levels[p] = st.levels;
+                launches[(size_t)q] += st.kernel_launches;
+            }
+        } catch (const Failure& e) {
+            fails[(size_t)q] = e;
+            stop = true;
+        } catch (const std::exception& e) {
+            fails[(size_t)q] = Failure{DGPU_CUDA_ERROR, e.what()};
+            stop = true;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int q = 1; q < S; ++q) pool.emplace_back(worker, q);
+    worker(0);
+    for (std::thread& t : pool) t.join();
+    for (const Failure& e : fails)
+        if (e.code != DGPU_OK) throw e;
+    // the context stream continues after every slot
+    for (int q = 0; q < S; ++q) {
+        CK(cudaEventRecord(C->slot_events[2 * (size_t)q + 1], C->slot_streams[(size_t)q]));
+        CK(cudaStreamWaitEvent(C->stream, C->slot_events[2 * (size_t)q + 1], 0));
+    }
+    CK(cudaEventRecord(C->ev1, C->stream));
+    CK(cudaEventSynchronize(C->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, C->ev0, C->ev1));
+    C->last_launches = std::accumulate(launches.begin(), launches.end(), (int64_t)0);
+    return ms;
 }
 
 // --------------------------------------------------------------- block solves
@@ -1296,6 +1434,9 @@ void dgpu_destroy(dgpu_context* ctx) {
         if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
         if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
         for (cudaEvent_t ev : ctx->chunk_events) cudaEventDestroy(ev);
+        ctx->slot_plans.clear();
+        for (cudaStream_t st : ctx->slot_streams) cudaStreamDestroy(st);
+        for (cudaEvent_t ev : ctx->slot_events) cudaEventDestroy(ev);
     }
     delete ctx;
 }
@@ -1339,6 +1480,13 @@ int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double
         std::vector<int> sides((size_t)batch, (int)n);
         dgpu_options o = *opt;
         o.record_history = 0;
+        if (route_to_grid(ctx, n, batch * n * n)) {  // large problems: concurrent grid-engine solves
+            std::vector<int64_t> order((size_t)batch);
+            std::iota(order.begin(), order.end(), (int64_t)0);
+            grid_solve_many(ctx, (int)n, order, offsets_of(sides), a, f, !f_per_sample, f_scalar, &o, u0, u_out,
+                            iterations, residuals, converged, levels, false);
+            return;
+        }
         BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
         block_solve(ctx, batch, sides, offsets_of(sides), a, f, f_per_sample ? 0 : 1, f_scalar, u0, &o, u_out, bo,
                     false, nullptr);
@@ -1364,6 +1512,14 @@ int dgpu_solve_batch_device(dgpu_context* ctx, const double* d_a, const double* 
         std::vector<int> sides((size_t)batch, (int)n);
         dgpu_options o = *opt;
         o.record_history = 0;
+        if (route_to_grid(ctx, n, batch * n * n)) {
+            std::vector<int64_t> order((size_t)batch);
+            std::iota(order.begin(), order.end(), (int64_t)0);
+            const float ms = grid_solve_many(ctx, (int)n, order, offsets_of(sides), d_a, d_f, !f_per_sample, f_scalar,
+                                             &o, d_u0, d_u, iterations, residuals, converged, levels, true);
+            if (device_ms) *device_ms = ms;
+            return;
+        }
         BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
         float ms = 0.f;
         block_solve(ctx, batch, sides, offsets_of(sides), d_a, d_f, f_per_sample ? 0 : 1, f_scalar, d_u0, &o, d_u, bo,
@@ -1372,6 +1528,8 @@ int dgpu_solve_batch_device(dgpu_context* ctx, const double* d_a, const double* 
         // block_solve synchronised the context stream: the caller's stream may continue
     });
 }
+
+int64_t dgpu_last_launches(const dgpu_context* ctx) { return ctx ? ctx->last_launches : 0; }
 
 int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, const double* a, const double* f,
                       double f_scalar, const dgpu_options* opt, const double* u0, double* u_out, int* iterations,
@@ -1389,12 +1547,14 @@ int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, co
         CK(cudaSetDevice(ctx->device));
         dgpu_options o = *opt;
         o.record_history = 0;
-        // Problems of side >= kGridEngineSide go to the grid engine, one
-        // graph-launched solve each, after the block engine has taken the
-        // rest: on one CTA such a problem would outlast the whole batch.
+        // Problems that one CTA would take longer on than the whole rest of
+        // the batch go to the grid engine (route_to_grid), after the block
+        // engine has taken the rest.
         const std::vector<int64_t> off = offsets_of(sv);
         std::vector<int64_t> small, big;
-        for (int64_t q = 0; q < count; ++q) (sv[q] >= kGridEngineSide ? big : small).push_back(q);
+        int64_t total = 0;
+        for (int v : sv) total += (int64_t)v * v;
+        for (int64_t q = 0; q < count; ++q) (route_to_grid(ctx, sv[q], total) ? big : small).push_back(q);
         if (big.empty()) {
             BatchOut bo{iterations, residuals, converged, levels, nullptr, nullptr};
             block_solve(ctx, count, sv, off, a, f, 0, f_scalar, u0, &o, u_out, bo, false, nullptr);
@@ -1419,16 +1579,17 @@ int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, co
             }
         }
         // (the block engine's copy-out covers the cells up to its last
-        // problem; the large problems' cells are written after it)
-        for (int64_t q : big) {
-            dgpu_stats st{};
-            grid_solve(ctx, a + off[q], f ? f + off[q] : nullptr, f_scalar, sv[q], &o, u0 ? u0 + off[q] : nullptr,
-                       u_out + off[q], nullptr, &st, false, nullptr);
-            iterations[q] = st.iterations;
-            residuals[q] = st.residual;
-            converged[q] = st.converged;
-            if (levels) levels[q] = st.levels;
+        // problem; the large problems' cells are written after it) -- large
+        // problems of one side at a time, concurrently
+        int64_t launched = small.empty() ? 0 : ctx->last_launches;
+        std::map<int, std::vector<int64_t>> by_side;
+        for (int64_t q : big) by_side[sv[q]].push_back(q);
+        for (auto it = by_side.rbegin(); it != by_side.rend(); ++it) {
+            grid_solve_many(ctx, it->first, it->second, off, a, f, false, f_scalar, &o, u0, u_out, iterations,
+                            residuals, converged, levels, false);
+            launched += ctx->last_launches;
         }
+        ctx->last_launches = launched;
     });
 }
 

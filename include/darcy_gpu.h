@@ -113,12 +113,18 @@ int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double
 
 /* Same, on device-resident arrays (d_a, d_f, d_u0, d_u: device pointers,
  * packed as above); per-sample results in host arrays; device_ms (may be
- * NULL) receives the device time of the solve. Ordered after `stream` (may be
+ * NULL) receives the device time of the solve. Problems too large for one
+ * CTA's share of the batch run as concurrent grid-engine solves, one stream
+ * each. Ordered after `stream` (may be
  * NULL); returns when the results are written. No reference counterpart. */
 int dgpu_solve_batch_device(dgpu_context* ctx, const double* d_a, const double* d_f, double f_scalar,
                             int f_per_sample, int64_t batch, int64_t n, const dgpu_options* opt, const double* d_u0,
                             double* d_u, int* iterations, double* residuals, int* converged, int* levels,
                             double* device_ms, void* stream);
+
+/* Kernels the context's last solve call launched on the device (a single
+ * solve, a batch of any engine, or a learned batch). No reference counterpart. */
+int64_t dgpu_last_launches(const dgpu_context* ctx);
 
 /* Uneven-size batch (additive extension of solve_batch): problem p has side
  * sides[p] and occupies cells [off_p, off_p + sides[p]^2) of the packed

@@ -398,6 +398,64 @@ def test_uneven_batch_routes_large_problems_to_the_grid_engine(darcy) -> None:
             assert rel_l2(out.u[q], single.u) < 1e-9
 
 
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_concurrent_grid_solves_equal_single_solves(darcy, monkeypatch, form) -> None:
+    """Batches of large problems run as concurrent grid-engine solves (one
+    plan, stream and host thread per slot). Lowering the routing side sends
+    small problems there too: every problem must come out bit-identical to
+    its own single solve (same graph, fixed reduction order), with f shared,
+    f per sample, x0, uneven sides grouped by side, and device buffers."""
+    from darcy_cpp_gb300 import capi
+
+    monkeypatch.setenv("DARCY_GPU_GRID_SIDE", "64")
+    monkeypatch.setenv("DARCY_GPU_SLOTS", "3")
+    ctx = capi.Context()
+    batch_a = np.stack([two_phase(96, seed=200 + q, hi=1e2, lo=1e-2) for q in range(7)])
+    f_shared = np.linspace(0.5, 1.5, 96 * 96).reshape(96, 96)
+    single = [ctx.solve(a, f_shared, form=form) for a in batch_a]
+    out = ctx.solve_batch(batch_a, f_shared, form=form)
+    for q in range(7):
+        assert out["iterations"][q] == single[q]["iterations"]
+        assert out["levels"][q] == single[q]["levels"]
+        assert np.array_equal(out["u"][q], single[q]["u"])
+    sides = [96, 40, 80, 96, 33, 80, 96]
+    fields = [two_phase(s, seed=300 + q) for q, s in enumerate(sides)]
+    fs = [np.full((s, s), 1.0 + 0.25 * q) for q, s in enumerate(sides)]
+    x0 = [np.full((s, s), 1e-4) for s in sides]
+    got = ctx.solve_uneven(fields, fs, x0=x0, form=form)
+    for q, (a, fq, xq) in enumerate(zip(fields, fs, x0)):
+        want = ctx.solve(a, fq, x0=xq, form=form)
+        assert got["converged"][q]
+        if sides[q] >= 64:  # grid engine: the single solve's own graph
+            assert got["iterations"][q] == want["iterations"]
+            assert np.array_equal(got["u"][q], want["u"])
+        else:  # block engine: same method, its own rounding
+            assert abs(got["iterations"][q] - want["iterations"]) <= 1
+            assert rel_l2(got["u"][q], want["u"]) < 1e-9
+    torch = pytest.importorskip("torch")
+    d_a = torch.from_numpy(batch_a).cuda()
+    d_u = torch.empty_like(d_a)
+    dev = ctx.solve_batch_device(d_a.data_ptr(), 7, 96, d_u.data_ptr(),
+                                 torch.cuda.current_stream().cuda_stream, form=form)
+    host = ctx.solve_batch(batch_a, 1.0, form=form)
+    assert np.array_equal(dev["iterations"], host["iterations"])
+    assert np.array_equal(d_u.cpu().numpy(), host["u"])
+    assert dev["device_ms"] > 0
+
+
+def test_concurrent_grid_solves_report_invalid_input(darcy, monkeypatch) -> None:
+    from darcy_cpp_gb300 import capi
+
+    monkeypatch.setenv("DARCY_GPU_GRID_SIDE", "16")
+    ctx = capi.Context()
+    batch_a = np.stack([np.full((20, 20), 2.0) for _ in range(5)])
+    batch_a[3, 2, 5] = np.nan
+    with pytest.raises(ValueError, match=f"positive.*flat index {2 * 20 + 5}"):
+        ctx.solve_batch(batch_a)
+    batch_a[3, 2, 5] = 2.0
+    assert ctx.solve_batch(batch_a)["converged"].all()  # the context stays usable
+
+
 def test_uneven_batch_matches_oracle(darcy, orc) -> None:
     sides = [32, 48, 64, 96, 128, 192, 256, 33, 17, 1, 2]
     fields = [two_phase(s, seed=10 + q) for q, s in enumerate(sides)]
