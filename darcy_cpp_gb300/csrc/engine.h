@@ -124,6 +124,8 @@ template <class T>
 void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s);
 template <class T>
 void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s);
+void launch_residual_restrict_df(const Lvl<float>& L, const float* elo, const float* nlo, const float* dlo,
+                                 const float* blo, float* bc, CgState* st, cudaStream_t s);
 template <class T>
 void launch_prolong_gs1(const Lvl<T>& L, const T* xc, CgState* st, cudaStream_t s);
 template <class T>

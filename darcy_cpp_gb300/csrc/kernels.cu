@@ -9,6 +9,7 @@
 #include <math.h>
 
 #include <cstdlib>
+#include <type_traits>
 
 #include "block.cuh"
 #include "cluster.cuh"
@@ -183,6 +184,47 @@ __global__ void k_residual_restrict(Lvl<T> L, T* bc, const CgState* st) {
     pdl_enter();
     if (st && st->done) return;
     residual_restrict<GridScope>(L, bc);
+}
+// The FP32 cycle's residual + restriction in double-float arithmetic on FP32
+// pipes: coefficients as hi + lo pairs, b with its lo part on level 0 (blo,
+// else null), error-free products and compensated sums, summed per 2 x 2
+// aggregate. Same operation order as the fused pre-visit (k_visit_pre), so
+// both give the same bits.
+__global__ void k_residual_restrict_df(Lvl<float> L, const float* __restrict__ elo, const float* __restrict__ nlo,
+                                       const float* __restrict__ dlo, const float* __restrict__ blo,
+                                       float* __restrict__ bc, const CgState* st) {
+    pdl_enter();
+    if (st && st->done) return;
+    const int n = L.n, nc = (n + 1) / 2;
+    const int64_t mc = (int64_t)nc * nc;
+    for (int64_t K = GridScope::start(); K < mc; K += GridScope::stride()) {
+        const int I = (int)(K / nc), J = (int)(K - (int64_t)I * nc);
+        DF acc{0.f, 0.f};
+        for (int di = 0; di < 2; ++di) {
+            const int i = 2 * I + di;
+            if (i >= n) break;
+            for (int dj = 0; dj < 2; ++dj) {
+                const int j = 2 * J + dj;
+                if (j >= n) break;
+                const int64_t k = (int64_t)i * n + j;
+                const float xe = j + 1 < n ? L.x[k + 1] : 0.f, ee = j + 1 < n ? L.e[k] : 0.f,
+                            el = j + 1 < n ? elo[k] : 0.f;
+                const float xw = j > 0 ? L.x[k - 1] : 0.f, ew = j > 0 ? L.e[k - 1] : 0.f,
+                            wl = j > 0 ? elo[k - 1] : 0.f;
+                const float xn = i + 1 < n ? L.x[k + n] : 0.f, en = i + 1 < n ? L.nf[k] : 0.f,
+                            nl = i + 1 < n ? nlo[k] : 0.f;
+                const float xs = i > 0 ? L.x[k - n] : 0.f, es = i > 0 ? L.nf[k - n] : 0.f,
+                            sl = i > 0 ? nlo[k - n] : 0.f;
+                df_add(acc, L.b[k], blo ? blo[k] : 0.f);
+                df_axpy(acc, L.d[k], dlo[k], L.x[k], -1.f);
+                df_axpy(acc, ee, el, xe, 1.f);
+                df_axpy(acc, ew, wl, xw, 1.f);
+                df_axpy(acc, en, nl, xn, 1.f);
+                df_axpy(acc, es, sl, xs, 1.f);
+            }
+        }
+        bc[K] = acc.hi + acc.lo;
+    }
 }
 template <class T>
 __global__ void k_prolong_gs1(Lvl<T> L, const T* xc, const CgState* st) {
@@ -415,9 +457,15 @@ __global__ void k_tail(const Lvl<T>* __restrict__ lv, int l0, int nlev, int pre,
 // unit vector e_j, computed by one CTA per column with the level vectors in
 // shared memory and the coefficients read from the (FP64) hierarchy. Stored
 // row-major, FP64 and optionally rounded to FP32 for the mixed form.
+// k_tail_matvec reads T before its programmatic-launch wait, so this kernel
+// waits for its predecessor but does not release its dependents early: the
+// next kernel starts only once T is complete. (Under programmatic launch a
+// kernel's pre-wait code overlaps only its immediate predecessor, which
+// itself started after the kernel before it had completed; data written two
+// or more kernels earlier is safe to read before the wait.)
 __global__ void k_tail_columns(const Lvl64* __restrict__ h, int l0, int nlev, int pre, int post, int gamma,
                                int top_calls, int N, double* __restrict__ Td, float* __restrict__ Tf) {
-    pdl_enter();
+    pdl_wait();
     extern __shared__ double sm_vec[];
     __shared__ Lvl<double> lv[kMaxLevels];
     if (threadIdx.x == 0) {
@@ -478,18 +526,53 @@ __device__ __forceinline__ T dot_row(const T* __restrict__ Mr, const T* __restri
     return warp_sum_t(acc);
 }
 
-// x_{l0} = T b_{l0}: one warp per row; the row streamed with 16-byte loads
-// (rows of N % 4 == 0 floats / N % 2 == 0 doubles; scalar otherwise), b read
-// through the read-only cache by every warp.
+// x_{l0} = T b_{l0}: one warp per row. T is constant during a solve, so when
+// a whole row fits in the warp's registers (N <= kTailRegCells, N a multiple
+// of the vector width) each warp loads its row before waiting for the kernel
+// that produces b: under programmatic launch that load overlaps the previous
+// kernel, and only the read of b is left between the two. Accumulation order
+// is dot_row's. Otherwise the row is prefetched to L2 and streamed.
+constexpr int kTailRegCells = 1024;  // the largest tail: a 32 x 32 level
+template <class T>
+__device__ __forceinline__ void tail_acc(T& acc, const float4& m, const float4& v) {
+    acc += (T)m.x * (T)v.x + (T)m.y * (T)v.y + (T)m.z * (T)v.z + (T)m.w * (T)v.w;
+}
+template <class T>
+__device__ __forceinline__ void tail_acc(T& acc, const double2& m, const double2& v) {
+    acc += (T)m.x * (T)v.x;
+    acc += (T)m.y * (T)v.y;
+}
 template <class T>
 __global__ void __launch_bounds__(128) k_tail_matvec(const T* __restrict__ M, int N, const T* __restrict__ b,
                                                      T* __restrict__ x, const CgState* st) {
     (void)st;  // scratch-only output: runs to completion even after convergence
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int kW = (int)(sizeof(V) / sizeof(T));
+    constexpr int kPer = kTailRegCells / (32 * kW);  // vectors per lane for a whole row
     const int lane = threadIdx.x & 31;
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-    // T is constant during a solve: bring this warp's first row towards the SM
-    // before waiting for the kernel that produces b.
+    if (N % kW == 0 && N <= kTailRegCells && nwarps >= N) {
+        const int nv = N / kW;
+        V mr[kPer];
+        if (warp < N) {
+            const V* Mr = reinterpret_cast<const V*>(M + (size_t)warp * N);
+#pragma unroll
+            for (int k = 0; k < kPer; ++k)
+                if (lane + 32 * k < nv) mr[k] = __ldg(Mr + lane + 32 * k);
+        }
+        pdl_enter();
+        if (warp < N) {
+            const V* bv = reinterpret_cast<const V*>(b);
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < kPer; ++k)
+                if (lane + 32 * k < nv) tail_acc<T>(acc, mr[k], __ldg(bv + lane + 32 * k));
+            acc = warp_sum_t(acc);
+            if (lane == 0) x[warp] = acc;
+        }
+        return;
+    }
     if (warp < N) {
         const char* row = reinterpret_cast<const char*>(M + (size_t)warp * N);
         for (int off = lane * 128; off < N * (int)sizeof(T); off += 32 * 128)
@@ -561,6 +644,11 @@ template <class T>
 void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s) {
     const int64_t nc = (L.n + 1) / 2;
     launch_k(k_residual_restrict<T>, grid_for(nc * nc), kThreads, 0, s, L, bc, st);
+}
+void launch_residual_restrict_df(const Lvl<float>& L, const float* elo, const float* nlo, const float* dlo,
+                                 const float* blo, float* bc, CgState* st, cudaStream_t s) {
+    const int64_t nc = (L.n + 1) / 2;
+    launch_k(k_residual_restrict_df, grid_for(nc * nc), kThreads, 0, s, L, elo, nlo, dlo, blo, bc, st);
 }
 template <class T>
 void launch_prolong_gs1(const Lvl<T>& L, const T* xc, CgState* st, cudaStream_t s) {

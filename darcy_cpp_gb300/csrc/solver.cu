@@ -75,6 +75,15 @@ constexpr int kTailSide = 32;
 // 1659 / 1344 ms with them routed (hence the share rule).
 constexpr int kGridEngineSide = 768;
 constexpr int kGridEngineMinSide = 384;
+// Grid-engine levels of at least this side run the unfused kernels (see
+// emit_visit_hybrid); smaller ones the fused visits. Measured on GB300
+// (mixed / FP64, ms per solve, all-fused -> unfused from this side):
+// 1024^2 at contrast 1e6 30.8 / 38.6 -> 30.6 / 36.9 (side 512: 32.1 / 38.1);
+// 2048^2 314 / 411 -> 275 / 364; 4096^2 at contrast 4 91.0 / 127 -> 71.4 / 108.
+// The fused visits stage a halo tile and run several barrier-separated
+// phases per tile, too few loads in flight to stream a large level; the
+// unfused kernels stream it at 60-98% of HBM bandwidth.
+constexpr int kUnfusedSide = 1024;
 // Concurrent grid-engine solves of a batch of large problems.
 constexpr int kGridSlots = 4;
 constexpr int kChunk = 8;  // iterations per launch when conditional nodes are unavailable
@@ -179,6 +188,7 @@ struct GridPlan {
     int64_t m = 0;
     bool mixed_mg = false;
     int cl0 = -1, cl_nl = 0, cl_ctas = 0;  // coarse levels run by one thread-block cluster (cl0 = top), or -1
+    int lf = 0;  // first level of the fused visits (the levels above it run the unfused kernels)
     Arena arena;
     double *a = nullptr, *f = nullptr, *u0 = nullptr, *u = nullptr;
     double *b = nullptr, *r = nullptr, *p = nullptr, *ap = nullptr, *z = nullptr;
@@ -261,6 +271,14 @@ namespace {
 
 // ------------------------------------------------------------ plan building
 
+// Levels of at least this side run the unfused kernels inside the fused
+// W-cycle (DARCY_GPU_UNFUSED_SIDE overrides).
+int unfused_side() {
+    const char* e = std::getenv("DARCY_GPU_UNFUSED_SIDE");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 ? v : kUnfusedSide;
+}
+
 void alloc_plan(dgpu_context* C, GridPlan& P) {
     const PlanKey& K = P.key;
     P.n = K.n;
@@ -324,6 +342,12 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
     P.nlo.assign(P.nlev, nullptr);
     P.dlo.assign(P.nlev, nullptr);
     P.fused = K.pre == 1 && K.post == 1;
+    P.lf = 0;
+    if (P.fused) {
+        const int side = unfused_side();
+        while (P.lf < P.tail_l0 && sides[P.lf] >= side) ++P.lf;
+        if (P.cl0 >= 0 && P.lf > P.cl0 - 1) P.lf = std::max(0, P.cl0 - 1);  // keep the cluster's parent fused
+    }
     auto layout = [&](Carver& A) {
         P.a = A.take<double>(m);
         P.f = A.take<double>(m);
@@ -438,7 +462,11 @@ void emit_visit(GridPlan& P, int l, bool first, cudaStream_t s) {
         launch_gs<T>(A, 0, first && q == 0, P.st, s);
         launch_gs<T>(A, 1, false, P.st, s);
     }
-    launch_residual_restrict<T>(A, lv[l + 1].b, P.st, s);
+    if constexpr (sizeof(T) == 4)  // the FP32 cycle restricts a double-float residual
+        launch_residual_restrict_df(A, P.elo[l], P.nlo[l], P.dlo[l], l == 0 ? P.b0lo : nullptr, lv[l + 1].b, P.st,
+                                    s);
+    else
+        launch_residual_restrict<T>(A, lv[l + 1].b, P.st, s);
     if (l + 1 >= P.tail_l0) {
         launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, lv[l + 1].x, P.st, s);
     } else {
@@ -491,9 +519,12 @@ void collect_visits(const GridPlan& P, int l, bool first, std::vector<VisitOp>& 
     ops.push_back({kOpPost, l, false});
 }
 
-std::vector<VisitOp> visit_program(const GridPlan& P) {
+// The fused ops of `calls` consecutive calls of level l_top (the first from a
+// zero iterate), a post-visit followed by the next pre-visit of the same
+// level merged into one mid-visit.
+std::vector<VisitOp> visit_program(const GridPlan& P, int l_top = 0, int calls = 1) {
     std::vector<VisitOp> raw, ops;
-    collect_visits(P, 0, true, raw);
+    for (int c = 0; c < calls; ++c) collect_visits(P, l_top, c == 0, raw);
     for (size_t i = 0; i < raw.size(); ++i) {
         if (raw[i].kind == kOpPost && i + 1 < raw.size() && raw[i + 1].kind == kOpPre && raw[i + 1].l == raw[i].l &&
             !raw[i + 1].first) {
@@ -507,11 +538,11 @@ std::vector<VisitOp> visit_program(const GridPlan& P) {
 }
 
 template <class T>
-void emit_visit_fused(GridPlan& P, std::vector<int>& cur, cudaStream_t s) {
+void emit_visit_fused(GridPlan& P, std::vector<int>& cur, cudaStream_t s, int l_top = 0, int calls = 1) {
     const auto& lv = levels_of<T>(P);
     const PlanKey& K = P.key;
     auto X = [&](int lvl, int q) { return (T*)(q == 0 ? P.X0[lvl] : P.X1[lvl]); };
-    for (const VisitOp& op : visit_program(P)) {
+    for (const VisitOp& op : visit_program(P, l_top, calls)) {
         const int l = op.l;
         const VisitLevel<T> V = visit_level<T>(P, l);
         switch (op.kind) {
@@ -555,6 +586,43 @@ void emit_visit_fused(GridPlan& P, std::vector<int>& cur, cudaStream_t s) {
     }
 }
 
+// Hybrid cycle: levels above P.lf (side >= kUnfusedSide) run the unfused
+// kernels (one per phase, streaming at a high fraction of HBM bandwidth),
+// the levels from P.lf down the fused visits (one launch per visit; the
+// small levels are latency-bound). Level l < P.lf works in place on lv[l].x;
+// the fused subtree below it leaves its result in X(P.lf, cur[P.lf]), which
+// the prolongation of level P.lf - 1 reads. Same arithmetic as the all-fused
+// program (the unfused kernels follow the fused ones' operation order).
+template <class T>
+void emit_visit_hybrid(GridPlan& P, int l, bool first, std::vector<int>& cur, cudaStream_t s) {
+    const auto& lv = levels_of<T>(P);
+    const PlanKey& K = P.key;
+    const Lvl<T>& A = lv[l];
+    launch_gs<T>(A, 0, first, P.st, s);
+    launch_gs<T>(A, 1, false, P.st, s);
+    if constexpr (sizeof(T) == 4)
+        launch_residual_restrict_df(A, P.elo[l], P.nlo[l], P.dlo[l], l == 0 ? P.b0lo : nullptr, lv[l + 1].b, P.st,
+                                    s);
+    else
+        launch_residual_restrict<T>(A, lv[l + 1].b, P.st, s);
+    const T* xc;
+    if (l + 1 >= P.tail_l0) {
+        launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, lv[l + 1].x, P.st, s);
+        xc = lv[l + 1].x;
+    } else if (l + 1 < P.lf) {
+        for (int g = 0; g < K.gamma; ++g) emit_visit_hybrid<T>(P, l + 1, g == 0, cur, s);
+        xc = lv[l + 1].x;
+    } else {
+        emit_visit_fused<T>(P, cur, s, l + 1, K.gamma);
+        xc = (const T*)(cur[l + 1] == 0 ? P.X0[l + 1] : P.X1[l + 1]);
+    }
+    launch_prolong_gs1<T>(A, xc, P.st, s);
+    if (l == 0)
+        launch_gs0_dot<T>(A, P.r, P.st, P.partials, s);
+    else
+        launch_gs<T>(A, 0, false, P.st, s);
+}
+
 void emit_setup(GridPlan& P, cudaStream_t s) {
     launch_build_fine(P.a, P.h[0], &P.st->bad, s);
     for (int l = 1; l < P.nlev; ++l) launch_coarsen(P.h[l - 1], P.h[l], s);
@@ -582,6 +650,13 @@ void emit_precondition(GridPlan& P, cudaStream_t s) {
                 launch_tail_matvec<double>(P.Td, P.ntail, P.r, P.z, P.st, s);
                 launch_dot_rz<double>(P.z, P.r, P.m, P.st, P.partials, s);
             }
+        } else if (P.fused && P.lf > 0) {
+            // unfused large levels; level 0 ends in place in lv[0].x: z / x0f
+            std::vector<int> cur(P.nlev, 0);
+            if (P.mixed_mg)
+                emit_visit_hybrid<float>(P, 0, true, cur, s);
+            else
+                emit_visit_hybrid<double>(P, 0, true, cur, s);
         } else if (P.fused) {
             // level 0 ends in X1[0] (pre writes X0, post writes X1): z / x0f
             std::vector<int> cur(P.nlev, 0);

@@ -368,6 +368,37 @@ def test_cluster_coarse_cycle_matches_per_visit_launches(darcy, monkeypatch, n) 
         assert rel_l2(z1, z0) < (1e-12 if form == "fp64" else 1e-5)
 
 
+@pytest.mark.parametrize("n", [65, 100, 256, 300])
+def test_hybrid_cycle_matches_fused_cycle(darcy, monkeypatch, n) -> None:
+    """Large levels on the unfused kernels, small ones on the fused visits
+    (DARCY_GPU_UNFUSED_SIDE): the same arithmetic in the same order. The FP32
+    cycle's output is bit-identical; in FP64 the compiler may fuse a different
+    product of d x - e x_E into the FMA in each kernel, so z agrees to
+    rounding. A solve also differs through the order of the r.z reduction
+    (iterations +-1, same solution to rounding)."""
+    from darcy_cpp_gb300 import capi
+
+    a = two_phase(n, seed=n + 7, hi=1e2, lo=1e-2)
+    r = np.random.default_rng(n).standard_normal((n, n))
+    monkeypatch.delenv("DARCY_GPU_UNFUSED_SIDE", raising=False)
+    fused = capi.Context()  # plans are built on first use: build them before the override
+    want = {form: (fused.apply_preconditioner(a, r, form=form), fused.solve(a, form=form))
+            for form in ("fp64", "mixed")}
+    for side in ("1", str(n // 2)):
+        monkeypatch.setenv("DARCY_GPU_UNFUSED_SIDE", side)
+        hybrid = capi.Context()
+        for form in ("fp64", "mixed"):
+            z0, s0 = want[form]
+            z1 = hybrid.apply_preconditioner(a, r, form=form)
+            if form == "mixed":
+                assert np.array_equal(z0, z1)
+            else:
+                assert rel_l2(z1, z0) < 1e-12
+            got = hybrid.solve(a, form=form)
+            assert got["converged"] and abs(got["iterations"] - s0["iterations"]) <= 1
+            assert rel_l2(got["u"], s0["u"]) < 1e-10
+
+
 def test_device_resident_batch_matches_host_batch(darcy) -> None:
     torch = pytest.importorskip("torch")
     from darcy_cpp_gb300 import capi
