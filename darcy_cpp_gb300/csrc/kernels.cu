@@ -10,6 +10,9 @@
 
 #include <cstdlib>
 #include <type_traits>
+#include <algorithm>
+#include <mutex>
+#include <map>
 
 #include "block.cuh"
 #include "cluster.cuh"
@@ -21,12 +24,33 @@ namespace dgpu {
 
 // ------------------------------------------------------------ small helpers
 
-// Grid of the streaming kernels: capped at 8 CTAs per SM (measured at
-// 1024^2: 608, 2432 and 4864 CTAs were all slower than 1216).
-static inline int grid_for(int64_t work, int threads = kThreads) {
+// Grid of the streaming (grid-stride) kernels: one wave of resident CTAs --
+// SMs x the CTAs per SM this kernel's registers allow -- or fewer when the
+// work is smaller, and never more than kMaxBlocks (the reduction partials).
+// A fixed 1216 (8 per SM) ran 1.33 waves for the 40-register kernels (6 CTAs
+// per SM): the last third of a wave took as long as a whole one.
+template <typename... KArgs>
+static int grid_fill(void (*kern)(KArgs...), int64_t work, int threads = kThreads) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> cap;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int c;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto key = std::make_pair((const void*)kern, dev);
+        auto it = cap.find(key);
+        if (it == cap.end()) {
+            int sms = 0, per = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, 0);
+            it = cap.emplace(key, std::max(1, std::min(kMaxBlocks, std::max(sms, 1) * std::max(per, 1)))).first;
+        }
+        c = it->second;
+    }
     int64_t g = (work + threads - 1) / threads;
     if (g < 1) g = 1;
-    if (g > kMaxBlocks) g = kMaxBlocks;
+    if (g > c) g = c;
     return (int)g;
 }
 
@@ -101,14 +125,14 @@ __global__ void k_to_fp32(Lvl64 L, float* e, float* nf, float* d, float* id, flo
 }
 
 void launch_build_fine(const double* a, const Lvl64& L, unsigned long long* bad, cudaStream_t s) {
-    launch_k(k_build_fine, grid_for((int64_t)L.n * L.n), kThreads, 0, s, a, L, bad);
+    launch_k(k_build_fine, grid_fill(k_build_fine, (int64_t)L.n * L.n), kThreads, 0, s, a, L, bad);
 }
 void launch_coarsen(const Lvl64& F, const Lvl64& C, cudaStream_t s) {
-    launch_k(k_coarsen, grid_for((int64_t)C.n * C.n), kThreads, 0, s, F, C);
+    launch_k(k_coarsen, grid_fill(k_coarsen, (int64_t)C.n * C.n), kThreads, 0, s, F, C);
 }
 void launch_to_fp32(const Lvl64& L, float* e, float* nf, float* d, float* id, float* elo, float* nlo, float* dlo,
                     cudaStream_t s) {
-    launch_k(k_to_fp32, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, e, nf, d, id, elo, nlo, dlo);
+    launch_k(k_to_fp32, grid_fill(k_to_fp32, (int64_t)L.n * L.n), kThreads, 0, s, L, e, nf, d, id, elo, nlo, dlo);
 }
 
 // ---------------------------------------------------------------- PCG kernels
@@ -634,29 +658,29 @@ void launch_visit_post(const VisitLevel<T>& V, const T* xin, const T* xc, T* xou
 void launch_cg_init(const double* f, double h2, int64_t m, double* b, double* r, double* u, double* p,
                     float* b0f, float* b0lo, const double* u0, const Lvl64& L0, CgState* st, double* partials,
                     cudaStream_t s) {
-    launch_k(k_cg_init, grid_for(m), kThreads, 0, s, f, h2, m, b, r, u, p, b0f, b0lo, u0, L0, st, partials);
+    launch_k(k_cg_init, grid_fill(k_cg_init, m), kThreads, 0, s, f, h2, m, b, r, u, p, b0f, b0lo, u0, L0, st, partials);
 }
 template <class T>
 void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s) {
-    launch_k(k_gs<T>, grid_for(colour_count(L.n, colour)), kThreads, 0, s, L, colour, zero, st);
+    launch_k(k_gs<T>, grid_fill(k_gs<T>, colour_count(L.n, colour)), kThreads, 0, s, L, colour, zero, st);
 }
 template <class T>
 void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s) {
     const int64_t nc = (L.n + 1) / 2;
-    launch_k(k_residual_restrict<T>, grid_for(nc * nc), kThreads, 0, s, L, bc, st);
+    launch_k(k_residual_restrict<T>, grid_fill(k_residual_restrict<T>, nc * nc), kThreads, 0, s, L, bc, st);
 }
 void launch_residual_restrict_df(const Lvl<float>& L, const float* elo, const float* nlo, const float* dlo,
                                  const float* blo, float* bc, CgState* st, cudaStream_t s) {
     const int64_t nc = (L.n + 1) / 2;
-    launch_k(k_residual_restrict_df, grid_for(nc * nc), kThreads, 0, s, L, elo, nlo, dlo, blo, bc, st);
+    launch_k(k_residual_restrict_df, grid_fill(k_residual_restrict_df, nc * nc), kThreads, 0, s, L, elo, nlo, dlo, blo, bc, st);
 }
 template <class T>
 void launch_prolong_gs1(const Lvl<T>& L, const T* xc, CgState* st, cudaStream_t s) {
-    launch_k(k_prolong_gs1<T>, grid_for(colour_count(L.n, 1)), kThreads, 0, s, L, xc, st);
+    launch_k(k_prolong_gs1<T>, grid_fill(k_prolong_gs1<T>, colour_count(L.n, 1)), kThreads, 0, s, L, xc, st);
 }
 template <class T>
 void launch_gs0_dot(const Lvl<T>& L, const double* r, CgState* st, double* partials, cudaStream_t s) {
-    launch_k(k_gs0_dot<T>, grid_for(colour_count(L.n, 0)), kThreads, 0, s, L, r, st, partials);
+    launch_k(k_gs0_dot<T>, grid_fill(k_gs0_dot<T>, colour_count(L.n, 0)), kThreads, 0, s, L, r, st, partials);
 }
 template <class T>
 void launch_tail(const Lvl<T>* lv_dev, int l0, int nlev, int pre, int post, int gamma, int top_calls,
@@ -679,38 +703,38 @@ void launch_tail_matvec(const T* M, int N, const T* b, T* x, CgState* st, cudaSt
 }
 template <class T>
 void launch_dot_rz(const T* z, const double* r, int64_t m, CgState* st, double* partials, cudaStream_t s) {
-    launch_k(k_dot_rz<T>, grid_for(m), kThreads, 0, s, z, r, m, st, partials);
+    launch_k(k_dot_rz<T>, grid_fill(k_dot_rz<T>, m), kThreads, 0, s, z, r, m, st, partials);
 }
 void launch_precond_diag(const double* r, const double* id, double* z, int64_t m, CgState* st,
                          double* partials, cudaStream_t s) {
-    launch_k(k_precond_diag, grid_for(m), kThreads, 0, s, r, id, z, m, st, partials);
+    launch_k(k_precond_diag, grid_fill(k_precond_diag, m), kThreads, 0, s, r, id, z, m, st, partials);
 }
 template <class Z>
 void launch_xpby(const Z* z, double* p, int64_t m, CgState* st, cudaStream_t s) {
-    launch_k(k_xpby<Z>, grid_for(m), kThreads, 0, s, z, p, m, st);
+    launch_k(k_xpby<Z>, grid_fill(k_xpby<Z>, m), kThreads, 0, s, z, p, m, st);
 }
 void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, double* partials,
                       cudaStream_t s) {
-    launch_k(k_apply_dot, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, p, ap, st, partials);
+    launch_k(k_apply_dot, grid_fill(k_apply_dot, (int64_t)L.n * L.n), kThreads, 0, s, L, p, ap, st, partials);
 }
 void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, float* b0lo,
                       const float* zold, int64_t m, CgState* st, double* partials, cudaStream_t s) {
-    launch_k(k_cg_update, grid_for(m), kThreads, 0, s, p, ap, u, r, b0f, b0lo, zold, m, st, partials);
+    launch_k(k_cg_update, grid_fill(k_cg_update, m), kThreads, 0, s, p, ap, u, r, b0f, b0lo, zold, m, st, partials);
 }
 void launch_true_residual(const Lvl64& L, const double* u, const double* b, double*, CgState* st,
                           double* partials, cudaStream_t s) {
-    launch_k(k_true_residual, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, const_cast<double*>(u), b, st, partials);
+    launch_k(k_true_residual, grid_fill(k_true_residual, (int64_t)L.n * L.n), kThreads, 0, s, L, const_cast<double*>(u), b, st, partials);
 }
 void launch_apply(const Lvl64& L, const double* x, double* y, cudaStream_t s) {
-    launch_k(k_apply, grid_for((int64_t)L.n * L.n), kThreads, 0, s, L, x, y);
+    launch_k(k_apply, grid_fill(k_apply, (int64_t)L.n * L.n), kThreads, 0, s, L, x, y);
 }
 template <class T>
 void launch_copy_cast(const double* src, T* dst, int64_t m, cudaStream_t s) {
-    launch_k(k_copy_cast<T>, grid_for(m), kThreads, 0, s, src, dst, m);
+    launch_k(k_copy_cast<T>, grid_fill(k_copy_cast<T>, m), kThreads, 0, s, src, dst, m);
 }
 template <class T>
 void launch_copy_back(const T* src, double* dst, int64_t m, cudaStream_t s) {
-    launch_k(k_copy_back<T>, grid_for(m), kThreads, 0, s, src, dst, m);
+    launch_k(k_copy_back<T>, grid_fill(k_copy_back<T>, m), kThreads, 0, s, src, dst, m);
 }
 
 // ================================================================ block engine

@@ -1874,27 +1874,38 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
             if (tail_l0 == 0) return;
             const Lvl<T> L1 = levels_of<T>(P)[1];
             const T* Tm = tail_matrix<T>(P);
-            // algorithmic bytes: every array the kernel must touch, once
+            // algorithmic bytes: every array the kernel must touch, once;
+            // launches per iteration 1 for the kernels level 0 runs (fused
+            // visits, or the unfused kernels from kUnfusedSide up), else 0
+            const bool l0_unfused = !P.fused || P.lf > 0;
+            const double on_f = l0_unfused ? 0.0 : 1.0, on_u = l0_unfused ? 1.0 : 0.0;
             if (P.fused) {
                 const VisitLevel<T> V0 = visit_level<T>(P, 0);
                 T* xa = (T*)P.X0[0];
                 T* xb = (T*)P.X1[0];
                 T* x1 = (T*)P.X0[1];
                 const double cb = sizeof(T) == 4 ? 7 * 4.0 : 4 * 8.0;  // staged coefficient bytes per cell
-                items.push_back({"visit_pre(l0)", cb * m + w * (2 * m + mc) + (sizeof(T) == 4 ? 4 * m : 0), 1.0,
+                items.push_back({"visit_pre(l0)", cb * m + w * (2 * m + mc) + (sizeof(T) == 4 ? 4 * m : 0), on_f,
                                  [=] { launch_visit_pre<T>(V0, nullptr, xa, L1.b, s); }});
-                items.push_back({"visit_post(l0)", 3 * w * m + w * (3 * m + mc) + 8 * m, 1.0, [=] {
+                items.push_back({"visit_post(l0)", 3 * w * m + w * (3 * m + mc) + 8 * m, on_f, [=] {
                                      launch_visit_post<T>(V0, xa, x1, xb, rvec, stp, partials, s);
                                  }});
             }
-            items.push_back({"gs_colour0_zero(l0)", w * m * 1.5, 1.0, [=] { launch_gs<T>(L0, 0, true, stp, s); }});
-            items.push_back({"gs_colour1(l0)", w * (m * 0.5 * 3 + m * 2 + m), 1.0,
+            items.push_back({"gs_colour0_zero(l0)", w * m * 1.5, on_u, [=] { launch_gs<T>(L0, 0, true, stp, s); }});
+            items.push_back({"gs_colour1(l0)", w * (m * 0.5 * 3 + m * 2 + m), on_u,
                              [=] { launch_gs<T>(L0, 1, false, stp, s); }});
-            items.push_back({"residual_restrict(l0)", w * (5 * m + mc), 1.0,
-                             [=] { launch_residual_restrict<T>(L0, L1.b, stp, s); }});
-            items.push_back({"prolong_gs1(l0)", w * (m * 0.5 * 3 + m * 2 + m + mc), 1.0,
+            if constexpr (sizeof(T) == 4) {  // double-float: e, nf, d and their lo parts, x, b, b_lo
+                const float *elo = P.elo[0], *nlo = P.nlo[0], *dlo = P.dlo[0], *blo = P.b0lo;
+                items.push_back({"residual_restrict(l0)", w * (8 * m + mc) + 4 * m, on_u, [=] {
+                                     launch_residual_restrict_df(L0, elo, nlo, dlo, blo, L1.b, stp, s);
+                                 }});
+            } else {
+                items.push_back({"residual_restrict(l0)", w * (5 * m + mc), on_u,
+                                 [=] { launch_residual_restrict<T>(L0, L1.b, stp, s); }});
+            }
+            items.push_back({"prolong_gs1(l0)", w * (m * 0.5 * 3 + m * 2 + m + mc), on_u,
                              [=] { launch_prolong_gs1<T>(L0, L1.x, stp, s); }});
-            items.push_back({"gs0_dot(l0)", w * (m * 0.5 * 3 + m * 2 + m) + 8 * m, 1.0,
+            items.push_back({"gs0_dot(l0)", w * (m * 0.5 * 3 + m * 2 + m) + 8 * m, on_u,
                              [=] { launch_gs0_dot<T>(L0, rvec, stp, partials, s); }});
             const double nt = (double)ntail;
             items.push_back({"tail_matvec", w * (nt * nt + 2 * nt), (double)visits_tail,
