@@ -81,6 +81,8 @@ def lib() -> ctypes.CDLL:
         L.dgpu_profile_kernels.argtypes = [_P, _P, ctypes.c_int64, ctypes.POINTER(Options), ctypes.c_int,
                                            ctypes.POINTER(KernelTime), ctypes.c_int, _I]
         L.dgpu_flush_l2.argtypes = [_P, ctypes.c_int64]
+        L.dgpu_check_conversions.argtypes = [_P, _P, ctypes.c_int64, _P, _P, _P, _P]
+        L.dgpu_check_conversions.restype = ctypes.c_int64
         L.dgpu_apply_preconditioner_noalloc.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                                         ctypes.c_int, _P, _P]
         L.dgpu_random_fields.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_ulonglong, ctypes.c_double,
@@ -283,6 +285,20 @@ class Context:
 
     def flush_l2(self, nbytes: int = 512 << 20) -> None:
         check(lib().dgpu_flush_l2(self.handle, int(nbytes)))
+
+    def check_conversions(self, x):
+        """The engine's integer-pipe FP64<->FP32 conversions on the values x:
+        (mismatches against the conversion instructions, hi, lo, rounded,
+        widened)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        hi = np.empty(x.size, np.float32)
+        lo = np.empty(x.size, np.float32)
+        rd = np.empty(x.size, np.float32)
+        wd = np.empty(x.size, np.float64)
+        mism = lib().dgpu_check_conversions(self.handle, _ptr(x), x.size, _ptr(hi), _ptr(lo), _ptr(rd), _ptr(wd))
+        if mism < 0:
+            check(-1)
+        return int(mism), hi, lo, rd, wd
 
     def solve_batch_learned(self, net: "Net", a, f: float = 1.0, **kw) -> dict:
         """solve_batch with the warm start predicted on the device by `net`."""

@@ -65,6 +65,69 @@ __device__ __forceinline__ void colour_cell(int n, int c, int64_t t, int& i, int
     }
 }
 
+// ------------------------------------------- FP64 <-> FP32 off the FP64 pipe
+//
+// GB300 issues FP64 arithmetic and FP64<->FP32 conversions at ~2 per SM per
+// clock (measured: 529 G FP64 FMA/s against 38.8 T FP32 FMA/s), so the mixed
+// form's conversions are done on the integer and FP32 pipes where the value is
+// in range, bit-identical to the conversion instructions (round to nearest,
+// ties to even); other values take the instructions.
+
+// hi = (float)x, lo = (float)(x - (double)hi): x as FP32 hi + lo. The 53-bit
+// significand is rounded to 24 bits on integers; the remainder x - hi is an
+// integer of at most 29 bits times 2^(e-52), rounded by one int->float
+// conversion and scaled by an exact power of two.
+__device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FFu) - 1023;
+    if (e < -74 || e > 126) {  // zero, tiny, huge, inf, nan
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+        return;
+    }
+    const unsigned long long sig = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned q = (unsigned)(sig >> 29);                 // leading 24 bits
+    const unsigned rem = (unsigned)sig & 0x1FFFFFFFu;   // trailing 29 bits
+    const bool up = rem > 0x10000000u || (rem == 0x10000000u && (q & 1u));
+    const int diff = (int)rem - (up ? 0x20000000 : 0);  // |x| - |hi| in units of 2^(e-52)
+    q += up ? 1u : 0u;
+    int eh = e;
+    if (q == (1u << 24)) {
+        q >>= 1;
+        ++eh;
+    }
+    const unsigned sgn = (unsigned)(bits >> 63) << 31;
+    hi = __uint_as_float(sgn | ((unsigned)(eh + 127) << 23) | (q & 0x7FFFFFu));
+    const float l = __int2float_rn(diff) * __uint_as_float((unsigned)(e - 52 + 127) << 23);
+    lo = diff == 0 ? 0.f : (sgn ? -l : l);  // x - hi == +0 when exact
+}
+
+// (float)x, the hi part of split_f64.
+__device__ __forceinline__ float round_f64(double x) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FFu) - 1023;
+    if (e < -126 || e > 126) return (float)x;
+    const unsigned long long sig = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned q = (unsigned)(sig >> 29);
+    const unsigned rem = (unsigned)sig & 0x1FFFFFFFu;
+    q += (rem > 0x10000000u || (rem == 0x10000000u && (q & 1u))) ? 1u : 0u;
+    int eh = e;
+    if (q == (1u << 24)) {
+        q >>= 1;
+        ++eh;
+    }
+    return __uint_as_float(((unsigned)(bits >> 63) << 31) | ((unsigned)(eh + 127) << 23) | (q & 0x7FFFFFu));
+}
+
+// (double)v, exact: the exponent rebiased and the significand shifted.
+__device__ __forceinline__ double widen_f32(float v) {
+    const unsigned b = __float_as_uint(v);
+    const unsigned ex = b & 0x7F800000u;
+    if (ex == 0u || ex == 0x7F800000u) return (double)v;  // zero, subnormal, inf, nan
+    return __hiloint2double((int)((b & 0x80000000u) | (((b >> 3) & 0x0FFFFFFFu) + 0x38000000u)), (int)(b << 29));
+}
+__device__ __forceinline__ double widen_f32(double v) { return v; }
+
 // ---------------------------------------------------------------- level ops
 //
 // Operation order follows the reference loops (level.hpp:105-161): the
@@ -190,13 +253,41 @@ __device__ __forceinline__ double block_sum(double v, double* scratch) {
     return t;
 }
 
+// Deterministic block sum with few FP64 instructions. GB300 issues FP64 adds
+// at ~1/64 of the FP32 rate, and a shuffle tree in every warp (five full-warp
+// adds per warp and value) cost as much FP64 issue as a streaming kernel's own
+// arithmetic at a few cells per thread (ncu: cg_update's FP64 pipe 71% busy
+// with 3 FMAs per cell). Here every thread stores its value, lane i of warp 0
+// adds values i, i + 32, ... (two interleaved chains, all lanes busy), then one
+// shuffle tree: blockDim/32 + 4 full-warp adds per block instead of
+// 5 blockDim/32 + 5. `scratch` holds blockDim.x doubles; blockDim.x is a
+// multiple of 64. Fixed order; every thread gets the total.
+__device__ __forceinline__ double block_sum_wide(double v, double* scratch) {
+    const int t = threadIdx.x, nw = (int)(blockDim.x >> 5);
+    __syncthreads();  // the previous call's readers are done with scratch
+    scratch[t] = v;
+    __syncthreads();
+    if (t < 32) {
+        double s0 = scratch[t], s1 = scratch[t + 32];
+        for (int w = 2; w < nw; w += 2) {
+            s0 += scratch[t + 32 * w];
+            s1 += scratch[t + 32 * (w + 1)];
+        }
+        const double s = warp_sum(s0 + s1);
+        if (t == 0) scratch[0] = s;
+    }
+    __syncthreads();
+    return scratch[0];
+}
+
 // Grid-wide deterministic sum: each block stores its partial, the last block
 // to finish (ticket counter) adds the partials in block order. Returns true in
-// every thread of the last block, with the total in `total`.
+// every thread of the last block, with the total in `total`. `scratch` holds
+// blockDim.x doubles (block_sum_wide).
 __device__ __forceinline__ bool grid_sum_last(double v, double* partials, unsigned* ticket, double* scratch,
                                               double& total) {
     __shared__ bool s_last;
-    const double bs = block_sum(v, scratch);
+    const double bs = block_sum_wide(v, scratch);
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = bs;
         __threadfence();
@@ -208,7 +299,7 @@ __device__ __forceinline__ bool grid_sum_last(double v, double* partials, unsign
     __threadfence();
     double acc = 0.0;
     for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) acc += ((volatile double*)partials)[q];
-    total = block_sum(acc, scratch);
+    total = block_sum_wide(acc, scratch);
     if (threadIdx.x == 0) *ticket = 0;  // ready for the next launch
     return true;
 }

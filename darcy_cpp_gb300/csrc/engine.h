@@ -161,6 +161,8 @@ void launch_cg_update(const double* p, const double* ap, double* u, double* r, f
 void launch_true_residual(const Lvl64& L, const double* u, const double* b, double* scratch, CgState* st,
                           double* partials, cudaStream_t s);
 void launch_apply(const Lvl64& L, const double* x, double* y, cudaStream_t s);
+void launch_check_conversions(const double* x, int64_t m, float* hi, float* lo, float* rounded, double* widened,
+                              unsigned long long* mismatches, cudaStream_t s);
 template <class T>
 void launch_copy_cast(const double* src, T* dst, int64_t m, cudaStream_t s);
 template <class T>

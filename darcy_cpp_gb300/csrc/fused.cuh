@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) k_visit_post(VisitLevel<T> V, const T* __
                                                     const double* __restrict__ r, CgState* st, double* partials) {
     constexpr int R = 2;
     using G = Tile<TH, TW, R>;
-    __shared__ double red[32];
+    __shared__ double red[256];  // block_sum_wide: one double per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* es = reinterpret_cast<T*>(smem_raw);
     T* ns = es + G::S;

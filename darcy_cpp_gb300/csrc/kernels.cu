@@ -88,8 +88,8 @@ __device__ __forceinline__ void stop_loop(CgState* st) {
 __device__ __forceinline__ bool grid_sum2_last(double v1, double v2, double* partials, unsigned* ticket,
                                                double* scratch, double& t1, double& t2) {
     __shared__ bool s_last;
-    const double b1 = block_sum(v1, scratch);
-    const double b2 = block_sum(v2, scratch);
+    const double b1 = block_sum_wide(v1, scratch);
+    const double b2 = block_sum_wide(v2, scratch);
     if (threadIdx.x == 0) {
         partials[2 * blockIdx.x] = b1;
         partials[2 * blockIdx.x + 1] = b2;
@@ -104,8 +104,8 @@ __device__ __forceinline__ bool grid_sum2_last(double v1, double v2, double* par
         a1 += ((volatile double*)partials)[2 * q];
         a2 += ((volatile double*)partials)[2 * q + 1];
     }
-    t1 = block_sum(a1, scratch);
-    t2 = block_sum(a2, scratch);
+    t1 = block_sum_wide(a1, scratch);
+    t2 = block_sum_wide(a2, scratch);
     if (threadIdx.x == 0) *ticket = 0;
     return true;
 }
@@ -144,7 +144,7 @@ __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
                           double* __restrict__ p, float* __restrict__ b0f, float* __restrict__ b0lo,
                           const double* __restrict__ u0, Lvl64 L0, CgState* st, double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     double sb = 0.0, sr = 0.0;
     const int n = L0.n;
     const double fscalar = st->fscalar;
@@ -162,9 +162,10 @@ __global__ void k_cg_init(const double* __restrict__ f, double h2, int64_t m,
         r[k] = rk;
         p[k] = 0.0;
         if (b0f) {
-            const float hi = (float)rk;
+            float hi, lo;
+            split_f64(rk, hi, lo);
             b0f[k] = hi;
-            b0lo[k] = (float)(rk - (double)hi);
+            b0lo[k] = lo;
         }
         sb += bk * bk;
         sr += rk * rk;
@@ -263,7 +264,7 @@ __global__ void k_prolong_gs1(Lvl<T> L, const T* xc, const CgState* st) {
 template <class T>
 __global__ void k_gs0_dot(Lvl<T> L, const double* __restrict__ r, CgState* st, double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     if (st->done) return;
     const int n = L.n;
     double acc = 0.0;
@@ -279,14 +280,14 @@ __global__ void k_gs0_dot(Lvl<T> L, const double* __restrict__ r, CgState* st, d
         if (i > 0) v += L.nf[k - n] * L.x[k - n];
         const T xn = v * L.id[k];
         L.x[k] = xn;
-        acc += r[k] * (double)xn;
+        acc += r[k] * widen_f32(xn);
     }
     const int64_t cnt1 = colour_count(n, 1);
     for (int64_t t = GridScope::start(); t < cnt1; t += GridScope::stride()) {
         int i, j;
         colour_cell(n, 1, t, i, j);
         const int64_t k = (int64_t)i * n + j;
-        acc += r[k] * (double)L.x[k];
+        acc += r[k] * widen_f32(L.x[k]);
     }
     double tot;
     if (!grid_sum_last(acc, partials, &st->ticket[1], red, tot)) return;
@@ -302,10 +303,10 @@ template <class T>
 __global__ void k_dot_rz(const T* __restrict__ z, const double* __restrict__ r, int64_t m, CgState* st,
                          double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     if (st->done) return;
     double acc = 0.0;
-    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) acc += r[k] * (double)z[k];
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) acc += r[k] * widen_f32(z[k]);
     double tot;
     if (!grid_sum_last(acc, partials, &st->ticket[1], red, tot)) return;
     if (threadIdx.x == 0) {
@@ -319,7 +320,7 @@ __global__ void k_dot_rz(const T* __restrict__ z, const double* __restrict__ r, 
 __global__ void k_precond_diag(const double* __restrict__ r, const double* __restrict__ id,
                                double* __restrict__ z, int64_t m, CgState* st, double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     if (st->done) return;
     double acc = 0.0;
     for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
@@ -345,14 +346,14 @@ __global__ void k_xpby(const Z* __restrict__ z, double* __restrict__ p, int64_t 
         return;
     }
     const double beta = st->beta;
-    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) p[k] = (double)z[k] + beta * p[k];
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) p[k] = widen_f32(z[k]) + beta * p[k];
 }
 
 // ap = A p and p . Ap, then alpha or a breakdown (solver.hpp:147-156).
 __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __restrict__ ap, CgState* st,
                             double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     if (st->done) return;
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
@@ -386,7 +387,7 @@ __global__ void k_cg_update(const double* __restrict__ p, const double* __restri
                             double* __restrict__ r, float* __restrict__ b0f, float* __restrict__ b0lo,
                             const float* __restrict__ zold, int64_t m, CgState* st, double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     if (st->done) return;
     const double alpha = st->alpha;
     double acc = 0.0, acc2 = 0.0;
@@ -395,15 +396,20 @@ __global__ void k_cg_update(const double* __restrict__ p, const double* __restri
         const double rk = r[k] - alpha * ap[k];
         r[k] = rk;
         if (b0f) {  // r as FP32 hi + lo for the FP32 cycle
-            const float hi = (float)rk;
+            float hi, lo;
+            split_f64(rk, hi, lo);
             b0f[k] = hi;
-            b0lo[k] = (float)(rk - (double)hi);
+            b0lo[k] = lo;
         }
-        if (zold) acc2 += rk * (double)zold[k];
+        if (zold) acc2 += rk * widen_f32(zold[k]);
         acc += rk * rk;
     }
-    double rr, rzo;
-    if (!grid_sum2_last(acc, acc2, partials, &st->ticket[3], red, rr, rzo)) return;
+    double rr, rzo = 0.0;
+    if (zold) {
+        if (!grid_sum2_last(acc, acc2, partials, &st->ticket[3], red, rr, rzo)) return;
+    } else if (!grid_sum_last(acc, partials, &st->ticket[3], red, rr)) {  // r.r alone: half the reduction
+        return;
+    }
     if (threadIdx.x == 0) {
         st->rzo = zold ? rzo : 0.0;
         const double res = sqrt(rr) / st->bnorm;
@@ -426,7 +432,7 @@ __global__ void k_cg_update(const double* __restrict__ p, const double* __restri
 __global__ void k_true_residual(Lvl64 L, double* __restrict__ u, const double* __restrict__ b, CgState* st,
                                 double* partials) {
     pdl_enter();
-    __shared__ double red[32];
+    __shared__ double red[kThreads];
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
     const bool zero_u = st->bnorm == 0.0;
@@ -453,6 +459,38 @@ __global__ void k_apply(Lvl64 L, const double* __restrict__ x, double* __restric
         const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
         y[k] = apply_cell(L, x, i, j);
     }
+}
+
+// The integer-pipe conversions of common.cuh against the conversion
+// instructions, element by element: hi/lo from split_f64, (float)x from
+// round_f64, (double)hi from widen_f32, and a count of elements where any of
+// them differs in its bits from the instruction form.
+__global__ void k_check_conversions(const double* __restrict__ x, int64_t m, float* __restrict__ hi,
+                                    float* __restrict__ lo, float* __restrict__ rounded,
+                                    double* __restrict__ widened, unsigned long long* mismatches) {
+    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+        const double v = x[k];
+        float h, l;
+        split_f64(v, h, l);
+        const float rd = round_f64(v);
+        const double w = widen_f32(h);
+        const float hi_ref = (float)v;
+        const float lo_ref = (float)(v - (double)hi_ref);
+        const double w_ref = (double)h;
+        const bool same = __float_as_uint(h) == __float_as_uint(hi_ref) && __float_as_uint(l) == __float_as_uint(lo_ref) &&
+                          __float_as_uint(rd) == __float_as_uint(hi_ref) &&
+                          __double_as_longlong(w) == __double_as_longlong(w_ref);
+        hi[k] = h;
+        lo[k] = l;
+        rounded[k] = rd;
+        widened[k] = w;
+        if (!same) atomicAdd(mismatches, 1ull);
+    }
+}
+void launch_check_conversions(const double* x, int64_t m, float* hi, float* lo, float* rounded, double* widened,
+                              unsigned long long* mismatches, cudaStream_t s) {
+    k_check_conversions<<<grid_fill(k_check_conversions, m), kThreads, 0, s>>>(x, m, hi, lo, rounded, widened,
+                                                                             mismatches);
 }
 
 template <class T>

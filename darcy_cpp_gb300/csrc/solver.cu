@@ -1933,23 +1933,36 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
                              launch_cg_update(pv, apv, uv, rw, f32 ? b0f : nullptr, b0lo, nullptr, mm, stp, partials,
                                               s);
                          }});
+        // DARCY_GPU_PROFILE_DIRECT=1 launches each kernel straight on the
+        // stream instead of from a graph, for a kernel profiler (which does
+        // not replay graph nodes of kernels that can end the CG loop).
+        const char* de = std::getenv("DARCY_GPU_PROFILE_DIRECT");
+        const bool direct = de && std::strcmp(de, "1") == 0;
         int q = 0;
         for (const Item& it : items) {
             if (q >= cap) break;
             CK(cudaMemcpyAsync(P.st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
-            cudaGraph_t g = capture(s, [&] {
-                for (int r = 0; r < reps; ++r) it.launch();
-            });
-            cudaGraphExec_t x;
-            CK(cudaGraphInstantiate(&x, g, 0));
-            cudaGraphDestroy(g);
-            CK(cudaGraphLaunch(x, s));  // warm
+            cudaGraphExec_t x = nullptr;
+            if (!direct) {
+                cudaGraph_t g = capture(s, [&] {
+                    for (int r = 0; r < reps; ++r) it.launch();
+                });
+                CK(cudaGraphInstantiate(&x, g, 0));
+                cudaGraphDestroy(g);
+            }
+            auto run_all = [&] {
+                if (x)
+                    CK(cudaGraphLaunch(x, s));
+                else
+                    for (int r = 0; r < reps; ++r) it.launch();
+            };
+            run_all();  // warm
             CK(cudaMemcpyAsync(P.st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
             CK(cudaEventRecord(ctx->ev0, s));
-            CK(cudaGraphLaunch(x, s));
+            run_all();
             CK(cudaEventRecord(ctx->ev1, s));
             CK(cudaStreamSynchronize(s));
-            cudaGraphExecDestroy(x);
+            if (x) cudaGraphExecDestroy(x);
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
             std::snprintf(out[q].name, sizeof out[q].name, "%s", it.name);
@@ -1971,6 +1984,39 @@ int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes) {
         CK(cudaMemsetAsync(p, 1, (size_t)bytes, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
     });
+}
+
+int64_t dgpu_check_conversions(dgpu_context* ctx, const double* x, int64_t count, float* hi, float* lo,
+                               float* rounded, double* widened) {
+    int64_t mism = -1;
+    const int rc = run([&] {
+        if (!ctx || !x || count < 1 || !hi || !lo || !rounded || !widened) invalid("bad arguments");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        const size_t m = (size_t)count;
+        // x, widened (8 B each), the mismatch counter, then hi, lo, rounded (4 B each)
+        char* base = ctx->misc.ensure(m * (8 + 8 + 4 + 4 + 4) + 8);
+        double* dx = (double*)base;
+        double* dw = dx + m;
+        unsigned long long* dm = (unsigned long long*)(dw + m);
+        float* dh = (float*)(dm + 1);
+        float* dl = dh + m;
+        float* dr = dl + m;
+        cudaStream_t s = ctx->stream;
+        CK(cudaMemcpyAsync(dx, x, m * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(dm, 0, sizeof(unsigned long long), s));
+        launch_check_conversions(dx, (int64_t)m, dh, dl, dr, dw, dm, s);
+        CK(cudaGetLastError());
+        unsigned long long hm = 0;
+        CK(cudaMemcpyAsync(hi, dh, m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(lo, dl, m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rounded, dr, m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(widened, dw, m * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&hm, dm, sizeof hm, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        mism = (int64_t)hm;
+    });
+    return rc == DGPU_OK ? mism : -1;
 }
 
 }  // extern "C"

@@ -3,11 +3,15 @@
     python -m darcy_cpp_gb300.profile_run solve --n 1024 --form mixed --reps 2
     python -m darcy_cpp_gb300.profile_run batch --n 64 --count 304 --form mixed
     python -m darcy_cpp_gb300.profile_run net --side 64 --count 256
+    python -m darcy_cpp_gb300.profile_run kernels --n 1024 --form mixed --reps 3
 
 `solve` is the 1024 x 1024 headline workload (two-phase field of seed 1,
 a in {1e3, 1e-3}; other sizes use seed 0 and {12, 3}); `batch` is the 64 x 64
 batched solve; `net` runs the warm-start network (a few training steps on
-solver-generated pairs, then one prediction). The CUDA-graph while loop of the
+solver-generated pairs, then one prediction); `kernels` times each finest-
+level kernel and the tail product back to back (dgpu_profile_kernels), each
+launched directly on the stream (DARCY_GPU_PROFILE_DIRECT=1) so that a kernel
+profiler sees the kernels that can end the CG loop too. The CUDA-graph while loop of the
 single solve cannot be replayed by a kernel profiler, so `solve` runs with the
 host-driven loop (DARCY_GPU_LOOP=host) unless --device-loop is given.
 """
@@ -22,7 +26,7 @@ import time
 
 def main(argv: list[str] | None = None) -> int:
     p = argparse.ArgumentParser(prog="python -m darcy_cpp_gb300.profile_run")
-    p.add_argument("workload", choices=["solve", "batch", "net"])
+    p.add_argument("workload", choices=["solve", "batch", "net", "kernels"])
     p.add_argument("--n", type=int, default=1024)
     p.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     p.add_argument("--reps", type=int, default=2)
@@ -31,8 +35,10 @@ def main(argv: list[str] | None = None) -> int:
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--device-loop", action="store_true")
     args = p.parse_args(argv)
-    if args.workload == "solve" and not args.device_loop:
+    if args.workload in ("solve", "kernels") and not args.device_loop:
         os.environ.setdefault("DARCY_GPU_LOOP", "host")
+    if args.workload == "kernels":
+        os.environ.setdefault("DARCY_GPU_PROFILE_DIRECT", "1")
 
     import numpy as np
 
@@ -45,6 +51,16 @@ def main(argv: list[str] | None = None) -> int:
         for _ in range(args.reps):
             r = darcy.solve(a, form=args.form)
         print(f"solve n={args.n} form={args.form}: {r.iterations} iterations, converged {r.converged}")
+    elif args.workload == "kernels":
+        from .capi import Context
+
+        big = args.n >= 1024
+        a = darcy.two_phase_permeability(darcy.gaussian_random_field(args.n, seed=1 if big else 0),
+                                         *((1e3, 1e-3) if big else (12.0, 3.0)))
+        rows = Context().profile_kernels(a, reps=args.reps, form=args.form)
+        for row in rows:
+            print(f"{row['name']:24s} {row['avg_ms'] * 1e3:9.2f} us  {row['bytes'] / 1e6:9.2f} MB  "
+                  f"x{row['launches_per_iteration']:g} per iteration")
     elif args.workload == "batch":
         b = np.stack([darcy.two_phase_permeability(darcy.gaussian_random_field(args.n, seed=s))
                       for s in range(args.count)])

@@ -177,6 +177,15 @@ int dgpu_apply_preconditioner_noalloc(const double* d_a, const double* d_r, int6
  * timed runs). */
 int dgpu_flush_l2(dgpu_context* ctx, int64_t bytes);
 
+/* Self-check of the engine's FP64<->FP32 conversions done on the integer and
+ * FP32 pipes (the mixed form's CG kernels use them in place of the conversion
+ * instructions): for each x[k] (host array), hi = (float)x, lo = (float)(x -
+ * hi), rounded = (float)x by the rounding-only helper, widened = (double)hi.
+ * Returns how many elements differ in any bit from the instruction forms, or
+ * -1 on error. Test hook; no counterpart in the reference. */
+int64_t dgpu_check_conversions(dgpu_context* ctx, const double* x, int64_t count, float* hi, float* lo,
+                               float* rounded, double* widened);
+
 /* Random two-phase fields on the GPU for training sets: the reference
  * generator's construction (python/darcy/fields.py:31-83: spectral amplitudes
  * tau^(alpha-1) (pi^2 |k|^2 + tau^2)^(-alpha/2), orthonormal inverse DCT,
