@@ -192,10 +192,10 @@ __device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& 
     if (!V.e || (const void*)V.e == (const void*)H.e) return;  // not visited / FP64 used in place
     const int64_t m = (int64_t)H.n * H.n;
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-        ((T*)V.e)[k] = (T)H.e[k];
-        ((T*)V.nf)[k] = (T)H.nf[k];
-        ((T*)V.d)[k] = (T)H.d[k];
-        ((T*)V.id)[k] = (T)H.id[k];
+        ((T*)V.e)[k] = narrow_to<T>(H.e[k]);
+        ((T*)V.nf)[k] = narrow_to<T>(H.nf[k]);
+        ((T*)V.d)[k] = narrow_to<T>(H.d[k]);
+        ((T*)V.id)[k] = narrow_to<T>(H.id[k]);
     }
 }
 
@@ -210,7 +210,7 @@ __device__ __forceinline__ double block_apply_dot(const Lvl64& L, const double* 
         y[k] = v;
         acc += x[k] * v;
     }
-    return block_sum(acc, red);
+    return block_sum_wide(acc, red);
 }
 
 // z = M r for one problem; returns r . z. For the FP32 cycle, r is rounded
@@ -225,12 +225,12 @@ __device__ double block_precondition(const BatchArgs& A, const BlockViews<T>& V,
         const double* id64 = V.h[V.nlev - 1].id;  // FP64 exact coarsest solve (no-tail hierarchies)
         if (sizeof(T) == 4) {
             if (!b_ready) {  // (the CG update usually wrote the rounded r already)
-                for (int64_t k = threadIdx.x; k < m; k += blockDim.x) V.lv[0].b[k] = (T)r[k];
+                for (int64_t k = threadIdx.x; k < m; k += blockDim.x) V.lv[0].b[k] = narrow_to<T>(r[k]);
                 __syncthreads();
             }
             block_cycle<T>(V.lv, 0, V.nlev, A.pre, A.post, A.gamma, 1, id64, V.tail, V.tl);
             for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-                const double zk = (double)V.lv[0].x[k];
+                const double zk = widen_f32(V.lv[0].x[k]);
                 z[k] = zk;
                 acc += r[k] * zk;
             }
@@ -245,7 +245,7 @@ __device__ double block_precondition(const BatchArgs& A, const BlockViews<T>& V,
             acc += r[k] * zk;
         }
     }
-    return block_sum(acc, red);
+    return block_sum_wide(acc, red);
 }
 
 // The dense tail of one problem: column j = the tail map applied to e_j, all

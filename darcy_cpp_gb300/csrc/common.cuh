@@ -73,16 +73,45 @@ __device__ __forceinline__ void colour_cell(int n, int c, int64_t t, int& i, int
 // in range, bit-identical to the conversion instructions (round to nearest,
 // ties to even); other values take the instructions.
 
+// The instruction forms for values outside the integer paths' range, kept out
+// of line: inlined, the compiler may evaluate them for every value and select,
+// which puts the FP64-pipe conversions back on the hot path.
+static __device__ __noinline__ float2 split_f64_slow(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+static __device__ __noinline__ float round_f64_slow(double x) { return (float)x; }
+static __device__ __noinline__ double widen_f32_slow(float v) { return (double)v; }
+
+// (float)i, rounded to nearest even, for |i| <= 2^28 without a conversion
+// instruction (GB300 issues int->float conversions on its narrow FP64 pipe):
+// i = h * 2^12 + l with l in [0, 4096) and |h| <= 2^16, each made exact from
+// its bits (2^23 + v has v as its low significand bits), then one FMA rounds
+// h * 4096 + l once.
+__device__ __forceinline__ float int29_to_float(int i) {
+    const int h = i >> 12;  // floor(i / 4096)
+    const unsigned l = (unsigned)i & 0xFFFu;
+    const float hf = __uint_as_float(0x4B000000u | (unsigned)(h + (1 << 20))) - 9437184.0f;  // 2^23 + 2^20
+    const float lf = __uint_as_float(0x4B000000u | l) - 8388608.0f;                         // 2^23
+    return __fmaf_rn(hf, 4096.0f, lf);
+}
+
 // hi = (float)x, lo = (float)(x - (double)hi): x as FP32 hi + lo. The 53-bit
 // significand is rounded to 24 bits on integers; the remainder x - hi is an
-// integer of at most 29 bits times 2^(e-52), rounded by one int->float
-// conversion and scaled by an exact power of two.
+// integer of at most 29 bits times 2^(e-52), rounded to FP32 by
+// int29_to_float and scaled by an exact power of two.
 __device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((bits >> 52) & 0x7FFu) - 1023;
-    if (e < -74 || e > 126) {  // zero, tiny, huge, inf, nan
-        hi = (float)x;
-        lo = (float)(x - (double)hi);
+    if (e < -74 || e > 126) {
+        if ((bits << 1) == 0ull) {  // +-0: hi keeps the sign, x - hi is +0
+            hi = __uint_as_float((unsigned)(bits >> 32));
+            lo = 0.f;
+        } else {  // tiny, huge, inf, nan
+            const float2 t = split_f64_slow(x);
+            hi = t.x;
+            lo = t.y;
+        }
         return;
     }
     const unsigned long long sig = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
@@ -98,7 +127,7 @@ __device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
     }
     const unsigned sgn = (unsigned)(bits >> 63) << 31;
     hi = __uint_as_float(sgn | ((unsigned)(eh + 127) << 23) | (q & 0x7FFFFFu));
-    const float l = __int2float_rn(diff) * __uint_as_float((unsigned)(e - 52 + 127) << 23);
+    const float l = int29_to_float(diff) * __uint_as_float((unsigned)(e - 52 + 127) << 23);
     lo = diff == 0 ? 0.f : (sgn ? -l : l);  // x - hi == +0 when exact
 }
 
@@ -106,7 +135,7 @@ __device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
 __device__ __forceinline__ float round_f64(double x) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((bits >> 52) & 0x7FFu) - 1023;
-    if (e < -126 || e > 126) return (float)x;
+    if (e < -126 || e > 126) return (bits << 1) == 0ull ? __uint_as_float((unsigned)(bits >> 32)) : round_f64_slow(x);
     const unsigned long long sig = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     unsigned q = (unsigned)(sig >> 29);
     const unsigned rem = (unsigned)sig & 0x1FFFFFFFu;
@@ -123,10 +152,20 @@ __device__ __forceinline__ float round_f64(double x) {
 __device__ __forceinline__ double widen_f32(float v) {
     const unsigned b = __float_as_uint(v);
     const unsigned ex = b & 0x7F800000u;
-    if (ex == 0u || ex == 0x7F800000u) return (double)v;  // zero, subnormal, inf, nan
+    if (ex == 0u || ex == 0x7F800000u)  // zero, subnormal, inf, nan
+        return (b << 1) == 0u ? __hiloint2double((int)b, 0) : widen_f32_slow(v);
     return __hiloint2double((int)((b & 0x80000000u) | (((b >> 3) & 0x0FFFFFFFu) + 0x38000000u)), (int)(b << 29));
 }
 __device__ __forceinline__ double widen_f32(double v) { return v; }
+
+// x in the cycle's precision T: round_f64 for FP32, x itself for FP64.
+template <class T>
+__device__ __forceinline__ T narrow_to(double x) {
+    if constexpr (sizeof(T) == 4)
+        return round_f64(x);
+    else
+        return x;
+}
 
 // ---------------------------------------------------------------- level ops
 //
@@ -230,27 +269,6 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
-}
-
-// Deterministic block sum: every thread gets the total. `scratch` holds at
-// least blockDim.x / 32 doubles. Fixed order, so repeated runs agree bit for bit.
-__device__ __forceinline__ double block_sum(double v, double* scratch) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nw = (blockDim.x + 31) >> 5;
-    v = warp_sum(v);
-    __syncthreads();
-    if (lane == 0) scratch[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (warp == 0) {
-        t = lane < nw ? scratch[lane] : 0.0;
-        t = warp_sum(t);
-        if (lane == 0) scratch[0] = t;
-    }
-    __syncthreads();
-    t = scratch[0];
-    __syncthreads();
-    return t;
 }
 
 // Deterministic block sum with few FP64 instructions. GB300 issues FP64 adds

@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(256) k_visit_post(VisitLevel<T> V, const T* __
                 const int k = gi * n + gj;
                 const T v = xs[(R + li) * G::SW + (R + lj)];
                 xout[k] = v;
-                if (r) acc += r[k] * (double)v;
+                if (r) acc += r[k] * widen_f32(v);
             }
         }
         __syncthreads();

@@ -383,6 +383,21 @@ __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __res
 // (Polak-Ribiere) beta: its FP32 cycle is a slightly inexact preconditioner,
 // and beta = r_new.(z_new - z_old) / r_old.z_old keeps CG's convergence rate
 // with it. For an exact preconditioner r_new . z_old = 0 and the two betas agree.
+//
+// kPairs: two adjacent cells per thread through 16-byte loads and stores, the
+// two pairs of a thread's two grid strides loaded before any arithmetic, so
+// more loads are in flight (a 1024^2 level gives a thread only ~3 cells).
+// Needs 16-byte aligned p, ap, u, r, 8-byte aligned b0f, b0lo, and no zold;
+// used for the FP64 form.
+__device__ __forceinline__ void cg_cell(double alpha, double pk, double apk, double& uk, double& rk, float* hi,
+                                        float* lo, double& acc) {
+    uk += alpha * pk;
+    rk = rk - alpha * apk;
+    if (hi) split_f64(rk, *hi, *lo);
+    acc += rk * rk;
+}
+
+template <bool kPairs>
 __global__ void k_cg_update(const double* __restrict__ p, const double* __restrict__ ap, double* __restrict__ u,
                             double* __restrict__ r, float* __restrict__ b0f, float* __restrict__ b0lo,
                             const float* __restrict__ zold, int64_t m, CgState* st, double* partials) {
@@ -391,6 +406,58 @@ __global__ void k_cg_update(const double* __restrict__ p, const double* __restri
     if (st->done) return;
     const double alpha = st->alpha;
     double acc = 0.0, acc2 = 0.0;
+    if constexpr (kPairs) {
+        const int64_t m2 = m >> 1, gs = GridScope::stride();
+        const double2* p2 = reinterpret_cast<const double2*>(p);
+        const double2* a2 = reinterpret_cast<const double2*>(ap);
+        double2* u2 = reinterpret_cast<double2*>(u);
+        double2* r2 = reinterpret_cast<double2*>(r);
+        const bool mixed = b0f != nullptr;
+        float2 hi, lo;
+        for (int64_t q0 = GridScope::start(); q0 < m2; q0 += 2 * gs) {
+            const int64_t q1 = q0 + gs;
+            const bool two = q1 < m2;
+            const double2 pa = p2[q0], aa = a2[q0];
+            double2 ua = u2[q0], ra = r2[q0];
+            double2 pb{0.0, 0.0}, ab{0.0, 0.0}, ub{0.0, 0.0}, rb{0.0, 0.0};
+            if (two) {
+                pb = p2[q1];
+                ab = a2[q1];
+                ub = u2[q1];
+                rb = r2[q1];
+            }
+            cg_cell(alpha, pa.x, aa.x, ua.x, ra.x, mixed ? &hi.x : nullptr, &lo.x, acc);
+            cg_cell(alpha, pa.y, aa.y, ua.y, ra.y, mixed ? &hi.y : nullptr, &lo.y, acc);
+            u2[q0] = ua;
+            r2[q0] = ra;
+            if (mixed) {
+                reinterpret_cast<float2*>(b0f)[q0] = hi;
+                reinterpret_cast<float2*>(b0lo)[q0] = lo;
+            }
+            if (two) {
+                cg_cell(alpha, pb.x, ab.x, ub.x, rb.x, mixed ? &hi.x : nullptr, &lo.x, acc);
+                cg_cell(alpha, pb.y, ab.y, ub.y, rb.y, mixed ? &hi.y : nullptr, &lo.y, acc);
+                u2[q1] = ub;
+                r2[q1] = rb;
+                if (mixed) {
+                    reinterpret_cast<float2*>(b0f)[q1] = hi;
+                    reinterpret_cast<float2*>(b0lo)[q1] = lo;
+                }
+            }
+        }
+        if ((m & 1) && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {  // odd m: the last cell
+            const int64_t k = m - 1;
+            double uk = u[k], rk = r[k];
+            float h, l;
+            cg_cell(alpha, p[k], ap[k], uk, rk, mixed ? &h : nullptr, &l, acc);
+            u[k] = uk;
+            r[k] = rk;
+            if (mixed) {
+                b0f[k] = h;
+                b0lo[k] = l;
+            }
+        }
+    } else
     for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
         u[k] += alpha * p[k];
         const double rk = r[k] - alpha * ap[k];
@@ -757,7 +824,16 @@ void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, 
 }
 void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, float* b0lo,
                       const float* zold, int64_t m, CgState* st, double* partials, cudaStream_t s) {
-    launch_k(k_cg_update, grid_fill(k_cg_update, m), kThreads, 0, s, p, ap, u, r, b0f, b0lo, zold, m, st, partials);
+    auto al = [](const void* q, uintptr_t a) { return ((uintptr_t)q & (a - 1)) == 0; };
+    // Pairs for the FP64 form (1024^2: 14.9 -> 12.8 us); the mixed form's
+    // pair kernel needs 72 registers and ran slower (18.8 -> 22.2 us).
+    const bool pairs = !zold && al(p, 16) && al(ap, 16) && al(u, 16) && al(r, 16) && al(b0f, 8) && al(b0lo, 8);
+    if (pairs)
+        launch_k(k_cg_update<true>, grid_fill(k_cg_update<true>, (m + 1) / 2), kThreads, 0, s, p, ap, u, r, b0f, b0lo,
+                 zold, m, st, partials);
+    else
+        launch_k(k_cg_update<false>, grid_fill(k_cg_update<false>, m), kThreads, 0, s, p, ap, u, r, b0f, b0lo, zold,
+                 m, st, partials);
 }
 void launch_true_residual(const Lvl64& L, const double* u, const double* b, double*, CgState* st,
                           double* partials, cudaStream_t s) {
@@ -825,7 +901,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         u[k] = u0 ? u0[k] : 0.0;
         sb += bk * bk;
     }
-    const double bnorm = sqrt(block_sum(sb, red));
+    const double bnorm = sqrt(block_sum_wide(sb, red));
     int iterations = 0, converged = 0;
     double residual = 0.0;
     if (bnorm == 0.0) {
@@ -852,7 +928,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             r[k] = rk;
             sr += rk * rk;
         }
-        residual = sqrt(block_sum(sr, red)) / bnorm;
+        residual = sqrt(block_sum_wide(sr, red)) / bnorm;
     } else {
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) r[k] = b[k];
         residual = 1.0;
@@ -863,6 +939,9 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
     if (residual < A.tol) {
         converged = 1;
     } else {
+        // (Leaving z in the FP32 iterate and widening it where p reads it, with
+        // no FP64 z array, measured 2% slower: 4096 x 64^2 mixed 23.1 against
+        // 22.7 ms.)
         double rz = block_precondition<T>(A, V, r, z, red);
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k];
         __syncthreads();
@@ -883,11 +962,11 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
                 const double rk = r[k] - alpha * ap[k];
                 r[k] = rk;
                 rr += rk * rk;
-                if (round_b) b32[k] = (T)rk;
+                if (round_b) b32[k] = narrow_to<T>(rk);
                 if (flexible) rzo += rk * z[k];  // z still holds the previous direction's z
             }
-            residual = sqrt(block_sum(rr, red)) / bnorm;
-            if (flexible) rzo = block_sum(rzo, red);
+            residual = sqrt(block_sum_wide(rr, red)) / bnorm;
+            if (flexible) rzo = block_sum_wide(rzo, red);
             iterations = it + 1;
             if (record && threadIdx.x == 0) A.history[it + 1] = residual;
             if (residual < A.tol) {
@@ -913,7 +992,7 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             const double rk = b[k] - apply_cell(h[0], u, i, j);
             tr += rk * rk;
         }
-        true_res = sqrt(block_sum(tr, red)) / bnorm;
+        true_res = sqrt(block_sum_wide(tr, red)) / bnorm;
     }
     if (A.u_host)
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) A.u_host[off + k] = u[k];
@@ -927,13 +1006,20 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
     }
 }
 
+// Dynamic shared memory of a block-engine CTA: the coarse-level budget, then
+// block_sum_wide's scratch, one double per thread.
+__host__ __device__ inline size_t block_red_offset(size_t budget) { return (budget + 15) & ~(size_t)15; }
+inline size_t block_smem_bytes(size_t budget, int threads) {
+    return block_red_offset(budget) + sizeof(double) * (size_t)threads;
+}
+
 template <class T>
 __global__ void __launch_bounds__(1024) k_block_solve(BatchArgs A) {
     __shared__ BlockViews<T> V;
-    __shared__ double red[32];
     __shared__ int s_pid;
     __shared__ unsigned long long s_bad;
     extern __shared__ __align__(16) unsigned char block_smem[];
+    double* red = reinterpret_cast<double*>(block_smem + block_red_offset(A.smem_budget));
     char* arena = A.scratch + (size_t)blockIdx.x * A.scratch_stride;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -952,15 +1038,17 @@ __global__ void __launch_bounds__(1024) k_block_solve(BatchArgs A) {
 template <class T>
 int block_solve_occupancy(int threads, size_t smem) {
     // static + dynamic shared memory above 48 KiB needs the opt-in, so set it always
-    cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t bytes = block_smem_bytes(smem, threads);
+    cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_block_solve<T>, threads, smem) != cudaSuccess) n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_block_solve<T>, threads, bytes) != cudaSuccess) n = 1;
     return n;
 }
 template <class T>
 void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream_t s) {
-    cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)args.smem_budget);
-    k_block_solve<T><<<ctas, threads, args.smem_budget, s>>>(args);
+    const size_t bytes = block_smem_bytes(args.smem_budget, threads);
+    cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    k_block_solve<T><<<ctas, threads, bytes, s>>>(args);
 }
 
 // ------------------------------------------------------ coarse-level cluster

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) k_precondition_noalloc(unsigned char* scr
                                                                int gamma, const double* __restrict__ a,
                                                                const double* __restrict__ r, double* __restrict__ z) {
     __shared__ BlockViews<double> V;
-    __shared__ double red[32];
+    __shared__ double red[256];  // block_sum_wide: one double per thread
     __shared__ unsigned long long s_bad;
     if (threadIdx.x == 0) carve<double>(n, (char*)scratch, nullptr, 0, &V);
     __syncthreads();

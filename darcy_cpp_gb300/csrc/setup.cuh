@@ -87,15 +87,18 @@ __device__ __forceinline__ void to_fp32(const Lvl64& L, float* e, float* nf, flo
                                         float* nlo, float* dlo) {
     const int64_t m = (int64_t)L.n * L.n;
     for (int64_t k = S::start(); k < m; k += S::stride()) {
-        const float eh = (float)L.e[k], nh = (float)L.nf[k], dh = (float)L.d[k];
+        float eh, el, nh, nl, dh, dl;  // split_f64: the conversions' bits without the FP64 pipe
+        split_f64(L.e[k], eh, el);
+        split_f64(L.nf[k], nh, nl);
+        split_f64(L.d[k], dh, dl);
         e[k] = eh;
         nf[k] = nh;
         d[k] = dh;
-        id[k] = (float)L.id[k];
+        id[k] = round_f64(L.id[k]);
         if (elo) {
-            elo[k] = (float)(L.e[k] - (double)eh);
-            nlo[k] = (float)(L.nf[k] - (double)nh);
-            dlo[k] = (float)(L.d[k] - (double)dh);
+            elo[k] = el;
+            nlo[k] = nl;
+            dlo[k] = dl;
         }
     }
 }
