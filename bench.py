@@ -141,6 +141,30 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def replica_max(values: list[float], world: int, device: str) -> list[float]:
+    """Each value's maximum over the replicas (one rank per GPU): a whole-job
+    time is its slowest replica's."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def job_ms_per_solve(slowest_ms: float, steps: int, solves_per_step: int, world: int) -> float:
+    """Whole-job ms/solve: the slowest replica's time over the solves of all
+    replicas (each replica solves the same workload: weak scaling)."""
+    return slowest_ms / (steps * solves_per_step * world)
+
+
+def job_solves_per_s(slowest_s: float, solves: int, world: int) -> float:
+    """Whole-job solves/s: the solves of all replicas over the slowest one's time."""
+    return solves * world / slowest_s
+
+
 def run_ours(args, rank: int, world: int) -> dict | None:
     import torch
 
@@ -256,18 +280,22 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             bdev[form] = min(runs)
         learned = run_learned(batch, flush)
     total_ms = {k: sum(v) for k, v in arms.items()}
-    if world > 1:
-        names = sorted(total_ms)
-        t = torch.tensor([total_ms[k] for k in names], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = {k: float(v) for k, v in zip(names, t)}
+    names = sorted(total_ms)
+    e2e_med = [statistics.median(e2e["mixed_batch"]), statistics.median(e2e["fp64_serial"])]
+    slowest = replica_max([total_ms[k] for k in names] + [bt["mixed"][0], bt["fp64"][0], bdev["mixed"],
+                                                          bdev["fp64"]] + e2e_med, world, f"cuda:{dev}")
+    total_ms = dict(zip(names, slowest[: len(names)]))
+    bt_s = {"mixed": slowest[len(names)], "fp64": slowest[len(names) + 1]}
+    bdev_ms = {"mixed": slowest[len(names) + 2], "fp64": slowest[len(names) + 3]}
+    e2e_slowest = {"mixed_batch": slowest[len(names) + 4], "fp64_serial": slowest[len(names) + 5]}
     if rank != 0:
         return None
 
-    per_solve = {k: v / (args.steps * nb) for k, v in total_ms.items()}  # ms/solve on each replica
+    # whole-job figures: the slowest replica's time over the solves of all replicas
+    per_solve = {k: job_ms_per_solve(v, args.steps, nb, world) for k, v in total_ms.items()}
     ms_mixed = per_solve["mixed_batch"]
     ms_fp64 = per_solve["fp64_serial"]
-    e2e_mixed = statistics.median(e2e["mixed_batch"]) / nb
+    e2e_mixed = job_ms_per_solve(e2e_slowest["mixed_batch"], 1, nb, world)
     serial_m, serial_p = res["mixed_serial"], res["fp64_serial"]
     batch_m = res["mixed_batch"]
     it_m = [int(v) for v in batch_m["iterations"]]
@@ -295,8 +323,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                 "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()} for p in prof]}
 
     cpu = run_cpu_baseline()
-    bsm = BATCH_SMALL / bt["mixed"][0]
-    bsp = BATCH_SMALL / bt["fp64"][0]
+    bsm = job_solves_per_s(bt_s["mixed"], BATCH_SMALL, world)
+    bsp = job_solves_per_s(bt_s["fp64"], BATCH_SMALL, world)
     line = {
         "metric": METRIC,
         "value": round(ms_mixed, 3),
@@ -304,7 +332,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(ms_mixed * nb, 3),
+        "ms_per_step": round(total_ms["mixed_batch"] / args.steps, 3),  # the slowest replica's step
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
@@ -315,7 +343,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "iterations": {"mixed": it_m, "fp64": it_p},
         "mixed_vs_fp64_rel_l2_max": mixed_err,
         "plain_fp64": {"value": round(ms_fp64, 3), "unit": "ms/solve", "how": "one solve per call, FP64",
-                       "e2e": round(statistics.median(e2e["fp64_serial"]) / nb, 3)},
+                       "e2e": round(job_ms_per_solve(e2e_slowest["fp64_serial"], 1, nb, world), 3)},
         "chosen_vs_plain": round(ms_fp64 / ms_mixed, 3),
         "split": {"fp64_batched": round(per_solve["fp64_batch"], 3),
                   "mixed_one_per_call": round(per_solve["mixed_serial"], 3), "unit": "ms/solve",
@@ -325,9 +353,9 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                     "chosen_vs_plain": round(bsm / bsp, 3),
                     "mean_iterations": float(bt["mixed"][1].iterations.mean()),
                     "e2e": True, "h2d_bytes": int(batch.nbytes), "d2h_bytes": int(batch.nbytes),
-                    "device_resident": {"mixed": round(BATCH_SMALL / bdev["mixed"] * 1e3, 1),
-                                        "fp64": round(BATCH_SMALL / bdev["fp64"] * 1e3, 1),
-                                        "chosen_vs_plain": round(bdev["fp64"] / bdev["mixed"], 3),
+                    "device_resident": {"mixed": round(job_solves_per_s(bdev_ms["mixed"] * 1e-3, BATCH_SMALL, world), 1),
+                                        "fp64": round(job_solves_per_s(bdev_ms["fp64"] * 1e-3, BATCH_SMALL, world), 1),
+                                        "chosen_vs_plain": round(bdev_ms["fp64"] / bdev_ms["mixed"], 3),
                                         "unit": "solves/s", "timing": "CUDA events, inputs in HBM"},
                     "mixed_learned": learned["solves_per_s"],
                     "learned_vs_plain": round(learned["solves_per_s"] / bsp, 3),
