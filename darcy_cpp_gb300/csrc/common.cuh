@@ -279,17 +279,17 @@ __device__ __forceinline__ double warp_sum(double v) {
 // adds values i, i + 32, ... (two interleaved chains, all lanes busy), then one
 // shuffle tree: blockDim/32 + 4 full-warp adds per block instead of
 // 5 blockDim/32 + 5. `scratch` holds blockDim.x doubles; blockDim.x is a
-// multiple of 64. Fixed order; every thread gets the total.
+// multiple of 32. Fixed order; every thread gets the total.
 __device__ __forceinline__ double block_sum_wide(double v, double* scratch) {
     const int t = threadIdx.x, nw = (int)(blockDim.x >> 5);
     __syncthreads();  // the previous call's readers are done with scratch
     scratch[t] = v;
     __syncthreads();
     if (t < 32) {
-        double s0 = scratch[t], s1 = scratch[t + 32];
+        double s0 = scratch[t], s1 = nw > 1 ? scratch[t + 32] : 0.0;
         for (int w = 2; w < nw; w += 2) {
             s0 += scratch[t + 32 * w];
-            s1 += scratch[t + 32 * (w + 1)];
+            if (w + 1 < nw) s1 += scratch[t + 32 * (w + 1)];
         }
         const double s = warp_sum(s0 + s1);
         if (t == 0) scratch[0] = s;

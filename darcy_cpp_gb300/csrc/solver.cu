@@ -1065,7 +1065,10 @@ void load_tuning(dgpu_context* C) {
         const std::string key = text.substr(pos + 1, end - pos - 1);
         int threads = 0;
         unsigned long long smem = 0;
-        if (std::sscanf(text.c_str() + end + 1, " : [ %d , %llu ]", &threads, &smem) == 2 && threads > 0)
+        // (a shape the kernel cannot take -- threads not a multiple of 32 in
+        // 32..1024, or more shared memory than a CTA has -- is ignored)
+        if (std::sscanf(text.c_str() + end + 1, " : [ %d , %llu ]", &threads, &smem) == 2 && threads >= 32 &&
+            threads <= 1024 && threads % 32 == 0 && smem <= 200ull * 1024)
             C->tuned[key] = BlockConfigPOD{threads, (size_t)smem};
         pos = end + 1;
     }

@@ -653,3 +653,49 @@ def test_integer_pipe_conversions_are_bit_identical(darcy) -> None:
     assert same(rd, hi_np)
     assert same(lo, lo_np)
     assert same(wd, hi_np.astype(np.float64))
+
+
+@pytest.mark.parametrize("threads", [32, 96, 160])
+def test_batched_engine_takes_any_whole_warp_count(darcy, monkeypatch, tmp_path, threads) -> None:
+    """The batched engine's block reductions work for any whole number of
+    warps (a tuning file may pin 1, 3 or 5 warps): same solutions as the
+    default launch shape, to rounding (the reduction order follows the shape)."""
+    import json
+
+    import torch
+    from darcy_cpp_gb300 import capi
+
+    batch_a = np.stack([two_phase(48, seed=s, hi=1e2, lo=1e-2) for s in range(6)])
+    want = capi.Context().solve_batch(batch_a, form="mixed")
+    tune = tmp_path / "tune.json"
+    key = f"{torch.cuda.get_device_name(0)}|side<=64|mixed|pc2|c2|s11"
+    tune.write_text(json.dumps({key: [threads, 16384]}))
+    monkeypatch.setenv("DARCY_GPU_TUNE_FILE", str(tune))
+    got = capi.Context().solve_batch(batch_a, form="mixed")
+    assert got["converged"].all()
+    assert np.all(np.abs(got["iterations"] - want["iterations"]) <= 1)
+    for q in range(len(batch_a)):
+        assert rel_l2(got["u"][q], want["u"][q]) < REL_L2
+
+
+def test_tuning_file_shapes_the_kernel_cannot_take_are_ignored(darcy, monkeypatch, tmp_path) -> None:
+    import json
+
+    import torch
+    from darcy_cpp_gb300 import capi
+
+    batch_a = np.stack([two_phase(40, seed=s) for s in range(4)])
+    empty = tmp_path / "empty.json"
+    empty.write_text("{}")
+    monkeypatch.setenv("DARCY_GPU_TUNE_FILE", str(empty))  # the default shape on both sides
+    want = capi.Context().solve_batch(batch_a, form="fp64")
+    tune = tmp_path / "tune.json"
+    dev = torch.cuda.get_device_name(0)
+    tune.write_text(json.dumps({f"{dev}|side<=64|fp64|pc2|c2|s11": [100, 16384],
+                                f"{dev}|side<=64|mixed|pc2|c2|s11": [256, 1 << 30]}))
+    monkeypatch.setenv("DARCY_GPU_TUNE_FILE", str(tune))
+    ctx = capi.Context()
+    got = ctx.solve_batch(batch_a, form="fp64")
+    assert np.array_equal(got["iterations"], want["iterations"])
+    assert np.allclose(got["u"], want["u"], rtol=0, atol=1e-13)
+    assert ctx.solve_batch(batch_a, form="mixed")["converged"].all()
