@@ -261,13 +261,45 @@ __global__ void k_prolong_gs1(Lvl<T> L, const T* xc, const CgState* st) {
 // Last post-smoothing pass on level 0 (colour 0) fused with rz = r . z and
 // beta = rz_new / rz (solver.hpp:167-171). z is the level-0 iterate; in the
 // mixed form it is the FP32 iterate widened to FP64 on the fly.
-template <class T>
+//
+// kPairs (even n): one thread per pair of horizontally adjacent cells, one of
+// each colour: the colour-0 one is updated (the same arithmetic as
+// gs_colour), both enter r . z, and r is read once as 16-byte pairs instead
+// of once per colour loop.
+template <class T, bool kPairs>
 __global__ void k_gs0_dot(Lvl<T> L, const double* __restrict__ r, CgState* st, double* partials) {
     pdl_enter();
     __shared__ double red[kThreads];
     if (st->done) return;
     const int n = L.n;
     double acc = 0.0;
+    if constexpr (kPairs) {
+        const int64_t m2 = (int64_t)n * n / 2;
+        for (int64_t q = GridScope::start(); q < m2; q += GridScope::stride()) {
+            const int k0 = (int)(2 * q);  // n^2 < 2^31
+            const int i = k0 / n, j0 = k0 - i * n;
+            const int jc = j0 + (i & 1);  // the colour-0 cell of the pair
+            const int kc = i * n + jc, ko = (i & 1) ? k0 : k0 + 1;
+            T v = L.b[kc];
+            if (jc + 1 < n) v += L.e[kc] * L.x[kc + 1];
+            if (jc > 0) v += L.e[kc - 1] * L.x[kc - 1];
+            if (i + 1 < n) v += L.nf[kc] * L.x[kc + n];
+            if (i > 0) v += L.nf[kc - n] * L.x[kc - n];
+            const T xn = v * L.id[kc];
+            const T xo = L.x[ko];
+            L.x[kc] = xn;
+            const double2 rv = reinterpret_cast<const double2*>(r)[q];
+            acc += rv.x * widen_f32((i & 1) ? xo : xn);
+            acc += rv.y * widen_f32((i & 1) ? xn : xo);
+        }
+        double tot;
+        if (!grid_sum_last(acc, partials, &st->ticket[1], red, tot)) return;
+        if (threadIdx.x == 0) {
+            st->beta = st->it == 0 ? 0.0 : (tot - st->rzo) / st->rz;
+            st->rz = tot;
+        }
+        return;
+    }
     const int64_t cnt0 = colour_count(n, 0);
     for (int64_t t = GridScope::start(); t < cnt0; t += GridScope::stride()) {
         int i, j;
@@ -350,6 +382,10 @@ __global__ void k_xpby(const Z* __restrict__ z, double* __restrict__ p, int64_t 
 }
 
 // ap = A p and p . Ap, then alpha or a breakdown (solver.hpp:147-156).
+//
+// kPairs: two consecutive cells per thread (two independent FP64 chains, one
+// 16-byte store of Ap); needs 16-byte aligned p and ap.
+template <bool kPairs>
 __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __restrict__ ap, CgState* st,
                             double* partials) {
     pdl_enter();
@@ -358,11 +394,31 @@ __global__ void k_apply_dot(Lvl64 L, const double* __restrict__ p, double* __res
     const int n = L.n;
     const int64_t m = (int64_t)n * n;
     double acc = 0.0;
-    for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
-        const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
-        const double y = apply_cell(L, p, i, j);
-        ap[k] = y;
-        acc += p[k] * y;
+    if constexpr (kPairs) {
+        const int64_t m2 = m >> 1;
+        for (int64_t q = GridScope::start(); q < m2; q += GridScope::stride()) {
+            const int k0 = (int)(2 * q);  // n^2 < 2^31
+            const int i0 = k0 / n, j0 = k0 - i0 * n;
+            const int i1 = j0 + 1 < n ? i0 : i0 + 1, j1 = j0 + 1 < n ? j0 + 1 : 0;
+            const double y0 = apply_cell(L, p, i0, j0);
+            const double y1 = apply_cell(L, p, i1, j1);
+            reinterpret_cast<double2*>(ap)[q] = make_double2(y0, y1);
+            const double2 pv = reinterpret_cast<const double2*>(p)[q];
+            acc += pv.x * y0;
+            acc += pv.y * y1;
+        }
+        if ((m & 1) && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {  // odd m: the last cell
+            const double y = apply_cell(L, p, n - 1, n - 1);
+            ap[m - 1] = y;
+            acc += p[m - 1] * y;
+        }
+    } else {
+        for (int64_t k = GridScope::start(); k < m; k += GridScope::stride()) {
+            const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
+            const double y = apply_cell(L, p, i, j);
+            ap[k] = y;
+            acc += p[k] * y;
+        }
     }
     double pap;
     if (!grid_sum_last(acc, partials, &st->ticket[2], red, pap)) return;
@@ -785,7 +841,12 @@ void launch_prolong_gs1(const Lvl<T>& L, const T* xc, CgState* st, cudaStream_t 
 }
 template <class T>
 void launch_gs0_dot(const Lvl<T>& L, const double* r, CgState* st, double* partials, cudaStream_t s) {
-    launch_k(k_gs0_dot<T>, grid_fill(k_gs0_dot<T>, colour_count(L.n, 0)), kThreads, 0, s, L, r, st, partials);
+    if ((L.n & 1) == 0 && ((uintptr_t)r & 15) == 0)
+        launch_k(k_gs0_dot<T, true>, grid_fill(k_gs0_dot<T, true>, colour_count(L.n, 0)), kThreads, 0, s, L, r, st,
+                 partials);
+    else
+        launch_k(k_gs0_dot<T, false>, grid_fill(k_gs0_dot<T, false>, colour_count(L.n, 0)), kThreads, 0, s, L, r, st,
+                 partials);
 }
 template <class T>
 void launch_tail(const Lvl<T>* lv_dev, int l0, int nlev, int pre, int post, int gamma, int top_calls,
@@ -820,7 +881,11 @@ void launch_xpby(const Z* z, double* p, int64_t m, CgState* st, cudaStream_t s) 
 }
 void launch_apply_dot(const Lvl64& L, const double* p, double* ap, CgState* st, double* partials,
                       cudaStream_t s) {
-    launch_k(k_apply_dot, grid_fill(k_apply_dot, (int64_t)L.n * L.n), kThreads, 0, s, L, p, ap, st, partials);
+    const int64_t m = (int64_t)L.n * L.n;
+    if ((((uintptr_t)p | (uintptr_t)ap) & 15) == 0)
+        launch_k(k_apply_dot<true>, grid_fill(k_apply_dot<true>, (m + 1) / 2), kThreads, 0, s, L, p, ap, st, partials);
+    else
+        launch_k(k_apply_dot<false>, grid_fill(k_apply_dot<false>, m), kThreads, 0, s, L, p, ap, st, partials);
 }
 void launch_cg_update(const double* p, const double* ap, double* u, double* r, float* b0f, float* b0lo,
                       const float* zold, int64_t m, CgState* st, double* partials, cudaStream_t s) {
