@@ -253,7 +253,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         bt = {}
         for form in ("mixed", "fp64"):
             runs = []
-            for _ in range(max(1, args.steps // 2)):
+            for _ in range(max(3, args.steps)):  # best of several: one 25-45 ms run is noisy
                 flush.zero_()
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
@@ -268,7 +268,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             ctx.solve_batch_device(d_batch.data_ptr(), BATCH_SMALL, N_SMALL, d_ub.data_ptr(), stream.cuda_stream,
                                    tol=TOL, form=form)  # tune
             runs = []
-            for _ in range(max(1, args.steps // 2)):
+            for _ in range(max(3, args.steps)):  # best of several: one 25-45 ms run is noisy
                 flush.zero_()
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)

@@ -1102,12 +1102,16 @@ size_t smem_budget_for(bool mixed) { return mixed ? 48 * 1024 : 96 * 1024; }
 // and fine-level coefficients live in global memory.
 constexpr size_t kSmemBudgetLarge = 180 * 1024;
 
-// Autotuning key of a batch (loads the tuning file on first use).
-std::string tune_key(dgpu_context* C, int maxside, bool mixed, const dgpu_options* o) {
-    char keybuf[160];
-    std::snprintf(keybuf, sizeof keybuf, "%s|side<=%d|%s|pc%d|c%d|s%d%d", C->device_name.c_str(),
+// Autotuning key of a batch (loads the tuning file on first use). Batches
+// too small to put 4 problems on every SM ("few") tune apart from larger ones
+// ("many"): the best shape differs (more threads per problem when problems
+// are scarce), and a shape tuned on a first small batch would otherwise be
+// reused for every large one.
+std::string tune_key(dgpu_context* C, int maxside, bool mixed, const dgpu_options* o, int64_t count) {
+    char keybuf[176];
+    std::snprintf(keybuf, sizeof keybuf, "%s|side<=%d|%s|pc%d|c%d|s%d%d|%s", C->device_name.c_str(),
                   size_bucket(maxside), mixed ? "mixed" : "fp64", o->preconditioner, o->cycle_index,
-                  o->pre_sweeps, o->post_sweeps);
+                  o->pre_sweeps, o->post_sweeps, count >= 4 * (int64_t)std::max(C->sms, 1) ? "many" : "few");
     load_tuning(C);
     return keybuf;
 }
@@ -1164,7 +1168,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     // tuned: the problems are split into a few chunks; chunk k + 1 is copied
     // in (copy stream) while chunk k runs, and each chunk's solutions are
     // copied out while the later chunks run.
-    const auto tuned_hit = C->tuned.find(tune_key(C, maxside, mixed, o));
+    const auto tuned_hit = C->tuned.find(tune_key(C, maxside, mixed, o, count));
     const int64_t resident = 2 * (int64_t)C->sms;
     const bool pipelined = !direct && !device_ptrs && !warm && tuned_hit != C->tuned.end() &&
                            count >= 4 * resident && !(o->record_history);
@@ -1224,7 +1228,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         CK(cudaGetLastError());
     };
 
-    const std::string key = tune_key(C, maxside, mixed, o);
+    const std::string key = tune_key(C, maxside, mixed, o, count);
     BlockConfig cfg;
     cfg.smem = smem_budget_for(mixed);
     auto hit = C->tuned.find(key);

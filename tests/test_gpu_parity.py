@@ -668,7 +668,7 @@ def test_batched_engine_takes_any_whole_warp_count(darcy, monkeypatch, tmp_path,
     batch_a = np.stack([two_phase(48, seed=s, hi=1e2, lo=1e-2) for s in range(6)])
     want = capi.Context().solve_batch(batch_a, form="mixed")
     tune = tmp_path / "tune.json"
-    key = f"{torch.cuda.get_device_name(0)}|side<=64|mixed|pc2|c2|s11"
+    key = f"{torch.cuda.get_device_name(0)}|side<=64|mixed|pc2|c2|s11|few"
     tune.write_text(json.dumps({key: [threads, 16384]}))
     monkeypatch.setenv("DARCY_GPU_TUNE_FILE", str(tune))
     got = capi.Context().solve_batch(batch_a, form="mixed")
@@ -691,8 +691,8 @@ def test_tuning_file_shapes_the_kernel_cannot_take_are_ignored(darcy, monkeypatc
     want = capi.Context().solve_batch(batch_a, form="fp64")
     tune = tmp_path / "tune.json"
     dev = torch.cuda.get_device_name(0)
-    tune.write_text(json.dumps({f"{dev}|side<=64|fp64|pc2|c2|s11": [100, 16384],
-                                f"{dev}|side<=64|mixed|pc2|c2|s11": [256, 1 << 30]}))
+    tune.write_text(json.dumps({f"{dev}|side<=64|fp64|pc2|c2|s11|few": [100, 16384],
+                                f"{dev}|side<=64|mixed|pc2|c2|s11|few": [256, 1 << 30]}))
     monkeypatch.setenv("DARCY_GPU_TUNE_FILE", str(tune))
     ctx = capi.Context()
     got = ctx.solve_batch(batch_a, form="fp64")
