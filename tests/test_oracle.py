@@ -2,8 +2,8 @@
 
 The golden vectors were produced by the reference itself (its headers compiled
 by oracle/build_ref.sh, one OpenMP thread) and its field generator; see
-tests/golden/make_golden.py. The oracle is the checker of every GPU parity
-test, so it must reproduce them exactly.
+tests/golden/make_golden.py. Every GPU parity test compares against the
+oracle, so it must reproduce them exactly.
 """
 
 from __future__ import annotations
