@@ -1229,8 +1229,19 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     };
 
     const std::string key = tune_key(C, maxside, mixed, o, count);
+    // Untuned default, and the autotuner's first candidate: 256 threads for
+    // small problems (4 CTAs per SM); 1024 when the batch holds problems of
+    // side >= 256, whose single-CTA solves dominate a launch (16384 x 128^2 +
+    // 64 x 512^2: 1.34 / 1.67 s mixed / FP64 with 1024 threads, 2.28 / 2.54 s
+    // with 256).
     BlockConfig cfg;
-    cfg.smem = smem_budget_for(mixed);
+    if (maxside >= 256) {
+        cfg.threads = 1024;
+        cfg.smem = 96 * 1024;
+    } else {
+        cfg.threads = 256;
+        cfg.smem = smem_budget_for(mixed);
+    }
     auto hit = C->tuned.find(key);
     if (hit != C->tuned.end()) {
         cfg.threads = hit->second.threads;
@@ -1245,26 +1256,43 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         float best = 1e30f;
         // (1024 threads: one problem per SM, half the resident arenas of 2 x 512,
         // for when the arenas of all resident problems outgrow the L2)
-        for (int threads : {128, 256, 512, 1024})
-            for (size_t smem : {(size_t)0, smem_budget_for(mixed), kSmemBudgetLarge}) {
-                if (smem == kSmemBudgetLarge && (!mixed || threads < 512)) continue;
-                const BlockConfig c{threads, smem};
-                launch(c, sample);  // warm (allocations, clocks)
-                float ms = 1e30f;
-                for (int rep = 0; rep < 2; ++rep) {  // best of two: one timing let noise pick the shape
-                    CK(cudaEventRecord(C->ev0, s));
-                    launch(c, sample);
-                    CK(cudaEventRecord(C->ev1, s));
-                    CK(cudaEventSynchronize(C->ev1));
-                    float t = 0.f;
-                    CK(cudaEventElapsedTime(&t, C->ev0, C->ev1));
-                    ms = std::min(ms, t);
-                }
-                if (ms < best) {
-                    best = ms;
-                    cfg = c;
-                }
+        std::vector<BlockConfig> cands{cfg};
+        auto add = [&](int threads, size_t smem) {
+            for (const BlockConfig& c : cands)
+                if (c.threads == threads && c.smem == smem) return;
+            cands.push_back(BlockConfig{threads, smem});
+        };
+        for (int threads : {128, 256, 512, 1024}) {
+            add(threads, 0);
+            add(threads, smem_budget_for(mixed));
+            if (threads == 1024) add(threads, 96 * 1024);
+            if (mixed && threads >= 512) add(threads, kSmemBudgetLarge);
+        }
+        // Time budget: each candidate costs three launches over the sample,
+        // and a launch lasts as long as its largest problem's single-CTA solve
+        // (over a second for 512^2). When the default's launch exceeds
+        // kTuneLaunchMs, tuning would cost more than it can save: keep the
+        // default.
+        constexpr float kTuneLaunchMs = 150.f;
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+            const BlockConfig c = cands[ci];
+            launch(c, sample);  // warm (allocations, clocks)
+            float ms = 1e30f;
+            for (int rep = 0; rep < 2; ++rep) {  // best of two: one timing let noise pick the shape
+                CK(cudaEventRecord(C->ev0, s));
+                launch(c, sample);
+                CK(cudaEventRecord(C->ev1, s));
+                CK(cudaEventSynchronize(C->ev1));
+                float t = 0.f;
+                CK(cudaEventElapsedTime(&t, C->ev0, C->ev1));
+                ms = std::min(ms, t);
             }
+            if (ms < best) {
+                best = ms;
+                cfg = c;
+            }
+            if (ci == 0 && ms > kTuneLaunchMs) break;
+        }
         C->tuned[key] = BlockConfigPOD{cfg.threads, cfg.smem};
         save_tuning(C);
     }
