@@ -202,7 +202,9 @@ def solve_batch_uneven(
 ) -> UnevenBatchResult:
     """Solve problems of different grid sizes together (one GPU launch).
 
-    ``f`` is a scalar for all problems or one scalar/array per problem.
+    ``f`` is a scalar for all problems or one scalar/array per problem. The
+    solutions ``u`` are views into one array (disjoint, writeable, C-ordered),
+    which stays alive while any of them does.
     """
     fl = list(fields)
     fa: Any = f

@@ -240,6 +240,7 @@ PYBIND11_MODULE(_core, m) {
             std::vector<int64_t> sides((size_t)count);
             std::vector<double> packed, fpacked, u0packed;
             std::vector<Array> keep;
+            keep.reserve((size_t)count);
             double fs = 0.0;
             const bool f_list = py::isinstance<py::list>(f) && py::len(f) == (size_t)count && count > 0 &&
                                 !py::isinstance<py::float_>(py::list(f)[0]);
@@ -249,11 +250,22 @@ PYBIND11_MODULE(_core, m) {
                 x0l = py::cast<py::list>(x0);
                 if ((int64_t)py::len(x0l) != count) throw InvalidInput("x0 must hold one array per field");
             }
+            // sizes first, so the packed input is allocated once (no regrowth
+            // of a multi-GB buffer)
+            size_t total = 0;
             for (int64_t q = 0; q < count; ++q) {
-                Array arr = py::cast<Array>(fields[q]);
-                auto buf = arr.request();
+                keep.push_back(py::cast<Array>(fields[q]));
+                auto buf = keep.back().request();
                 const int64_t n = require_square_2d(buf, "each field");
                 sides[q] = n;
+                total += (size_t)(n * n);
+            }
+            packed.reserve(total);
+            if (f_list) fpacked.reserve(total);
+            if (!x0.is_none()) u0packed.reserve(total);
+            for (int64_t q = 0; q < count; ++q) {
+                auto buf = keep[(size_t)q].request();
+                const int64_t n = sides[q];
                 const auto* p = static_cast<const double*>(buf.ptr);
                 packed.insert(packed.end(), p, p + n * n);
                 if (f_list) {
@@ -267,25 +279,27 @@ PYBIND11_MODULE(_core, m) {
                     u0packed.insert(u0packed.end(), v.begin(), v.end());
                 }
             }
-            std::vector<double> u(packed.size()), res((size_t)count);
+            // the solutions land in one array; each problem's u is a view of it
+            py::array_t<double> ubig = new_array({(py::ssize_t)total});
+            double* up = static_cast<double*>(ubig.request().ptr);
+            std::vector<double> res((size_t)count);
             std::vector<int> iters((size_t)count), conv((size_t)count), levels((size_t)count);
             int rc;
             {
                 py::gil_scoped_release release;
                 rc = dgpu_solve_uneven(context(), count, sides.data(), packed.data(),
                                        fpacked.empty() ? nullptr : fpacked.data(), fs, &o,
-                                       u0packed.empty() ? nullptr : u0packed.data(), u.data(), iters.data(),
+                                       u0packed.empty() ? nullptr : u0packed.data(), up, iters.data(),
                                        res.data(), conv.data(), levels.data());
             }
             check(rc);
             py::list us;
             size_t off = 0;
             for (int64_t q = 0; q < count; ++q) {
-                const int64_t n = sides[q];
-                py::array_t<double> arr = new_array({(py::ssize_t)n, (py::ssize_t)n});
-                std::memcpy(arr.request().ptr, u.data() + off, sizeof(double) * (size_t)(n * n));
+                const py::ssize_t n = (py::ssize_t)sides[q];
+                us.append(py::array_t<double>({n, n}, {n * (py::ssize_t)sizeof(double), (py::ssize_t)sizeof(double)},
+                                              up + off, ubig));
                 off += (size_t)(n * n);
-                us.append(arr);
             }
             std::vector<bool> c(conv.begin(), conv.end());
             return py::make_tuple(us, iters, res, c, levels);
