@@ -186,7 +186,10 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
 }
 
 // Cycle coefficients of level l in the cycle's precision (FP32 copies for the
-// mixed form, shared-memory copies for the levels held on chip).
+// mixed form, shared-memory copies for the levels held on chip). The FP32
+// reciprocal diagonal is the correctly rounded reciprocal of the FP32 d (the
+// FP64 id is not built for FP32 cycles: it cost three FP64 divisions per
+// cell of setup); FP64 copies take id as built.
 template <class T>
 __device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& V) {
     if (!V.e || (const void*)V.e == (const void*)H.e) return;  // not visited / FP64 used in place
@@ -194,8 +197,12 @@ __device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& 
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
         ((T*)V.e)[k] = narrow_to<T>(H.e[k]);
         ((T*)V.nf)[k] = narrow_to<T>(H.nf[k]);
-        ((T*)V.d)[k] = narrow_to<T>(H.d[k]);
-        ((T*)V.id)[k] = narrow_to<T>(H.id[k]);
+        const T dk = narrow_to<T>(H.d[k]);
+        ((T*)V.d)[k] = dk;
+        if constexpr (sizeof(T) == 4)
+            ((T*)V.id)[k] = __frcp_rn(dk);
+        else
+            ((T*)V.id)[k] = H.id[k];
     }
 }
 
@@ -276,10 +283,12 @@ __device__ unsigned long long block_setup(const BatchArgs& A, const double* a, c
                                           unsigned long long* s_bad) {
     if (threadIdx.x == 0) *s_bad = ~0ull;
     __syncthreads();
-    build_fine<BlockScope>(a, V.h[0], s_bad);
-    __syncthreads();
+    // FP64 reciprocal diagonals: every level for an FP64 cycle; level 0 for
+    // the Jacobi preconditioner; otherwise the coarsest level's exact solve only.
+    const bool fp64_id = sizeof(T) == 8 || A.pc != kPcMultigrid;
+    build_fine_block(a, V.h[0], s_bad, fp64_id || V.nlev == 1);
     for (int l = 1; l < V.nlev; ++l) {
-        coarsen<BlockScope>(V.h[l - 1], V.h[l]);
+        coarsen<BlockScope>(V.h[l - 1], V.h[l], fp64_id || l == V.nlev - 1);
         __syncthreads();
     }
     if (A.pc == kPcMultigrid) {

@@ -1,5 +1,6 @@
-// Hierarchy construction on the device, always in FP64 (the Galerkin sums
-// and the reciprocal diagonal are the steps whose accuracy the cycle rests on).
+// Hierarchy construction on the device, in FP64 (the Galerkin sums and the
+// reciprocal diagonal are the steps whose accuracy the cycle rests on; an FP32
+// cycle takes its reciprocal diagonal from the FP32 copy of d instead).
 #pragma once
 
 #include <math.h>
@@ -48,12 +49,46 @@ __device__ __forceinline__ void build_fine(const double* __restrict__ a, const L
     }
 }
 
+// build_fine for one CTA with every face computed once (one division per
+// face instead of two; FP64 division is tens of instructions on the narrow
+// FP64 pipe): the east/north faces and the boundary faces first, then the
+// diagonal from the stored faces in build_fine's summation order. A cell's
+// west/south face is its neighbour's east/north face, the same bits since
+// harmonic() is symmetric, so the level equals build_fine's bit for bit.
+// with_id false leaves id unwritten (the FP32 cycle computes its own
+// reciprocal from the FP32 diagonal). Returns with the CTA synchronised.
+__device__ __forceinline__ void build_fine_block(const double* __restrict__ a, const Lvl64& L,
+                                                 unsigned long long* bad, bool with_id) {
+    const int n = L.n;
+    const int64_t m = (int64_t)n * n;
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double c = a[k];
+        if (!(c > 0.0) || !isfinite(c)) atomicMin(bad, (unsigned long long)k);
+        L.e[k] = (j + 1 < n) ? harmonic(c, a[k + 1]) : c;
+        L.nf[k] = (i + 1 < n) ? harmonic(c, a[k + n]) : c;
+        if (j == 0) L.wb[i] = c;
+        if (i == 0) L.sb[j] = c;
+    }
+    __syncthreads();
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const int i = (int)(k / n), j = (int)(k - (int64_t)i * n);
+        const double w = (j > 0) ? L.e[k - 1] : L.wb[i];
+        const double s = (i > 0) ? L.nf[k - n] : L.sb[j];
+        const double dd = L.e[k] + w + L.nf[k] + s;
+        L.d[k] = dd;
+        if (with_id) L.id[k] = 1.0 / dd;
+    }
+    __syncthreads();
+}
+
 // Galerkin coarse operator P^T A P by face summation (level.hpp:171-211),
 // including the width-one trailing aggregate of an odd grid. West/south fine
 // faces come from the neighbour's east/north face (same bits) or, on the
-// domain boundary, from wb/sb; summation order is the reference's.
+// domain boundary, from wb/sb; summation order is the reference's. with_id
+// false leaves id unwritten, as in build_fine_block.
 template <class S>
-__device__ __forceinline__ void coarsen(const Lvl64& F, const Lvl64& C) {
+__device__ __forceinline__ void coarsen(const Lvl64& F, const Lvl64& C, bool with_id = true) {
     const int n = F.n, nc = C.n;
     const int64_t mc = (int64_t)nc * nc;
     for (int64_t K = S::start(); K < mc; K += S::stride()) {
@@ -73,7 +108,7 @@ __device__ __forceinline__ void coarsen(const Lvl64& F, const Lvl64& C) {
         C.e[K] = ce;
         C.nf[K] = cn;
         C.d[K] = dd;
-        C.id[K] = 1.0 / dd;
+        if (with_id) C.id[K] = 1.0 / dd;
         if (J == 0) C.wb[I] = cw;
         if (I == 0) C.sb[J] = cs;
     }
