@@ -92,7 +92,10 @@ int dgpu_device_info(dgpu_context* ctx, char* out, int capacity);
 /* darcy::solve, reference solver.hpp:83-174 behind _core.solve
  * (src/bindings.cpp:117-138). a: n*n permeability; f: n*n forcing or NULL to
  * use f_scalar everywhere (bindings.cpp:51-63); u0: n*n warm start or NULL
- * (additive extension); u_out: n*n; history_out: NULL or max_iter + 1. */
+ * (additive extension); u_out: n*n; history_out: NULL or max_iter + 1.
+ * Host u_out buffers are written while the GPU computes (one element per
+ * page, so that the copy out finds its pages mapped): they must not alias an
+ * input. The same holds for every host-array entry point below. */
 int dgpu_solve(dgpu_context* ctx, const double* a, const double* f, double f_scalar, int64_t n,
                const dgpu_options* opt, const double* u0, double* u_out, double* history_out,
                dgpu_stats* stats);
