@@ -188,8 +188,8 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
 // Cycle coefficients of level l in the cycle's precision (FP32 copies for the
 // mixed form, shared-memory copies for the levels held on chip). The FP32
 // reciprocal diagonal is the correctly rounded reciprocal of the FP32 d (the
-// FP64 id is not built for FP32 cycles: it cost three FP64 divisions per
-// cell of setup); FP64 copies take id as built.
+// FP64 id, one FP64 division per cell, is built for FP32 cycles on the
+// coarsest level only); FP64 copies take id as built.
 template <class T>
 __device__ __forceinline__ void block_copy_coeffs(const Lvl64& H, const Lvl<T>& V) {
     if (!V.e || (const void*)V.e == (const void*)H.e) return;  // not visited / FP64 used in place
