@@ -810,8 +810,14 @@ void check_options(int64_t n, const dgpu_options* o) {
 // produce the data: ~1.5 ms for the last 33 MB chunk of a pipelined batch.
 // Touching one element per page while the GPU still computes takes that off
 // the critical path; on pages already mapped the loop costs a few
-// microseconds. The range is output only (the copy overwrites it).
+// microseconds. The range is output only (the copy overwrites it). A device
+// pointer passed where host memory belongs is left to the copy to report.
 void prefault_output(double* p, int64_t count) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess)
+        (void)cudaGetLastError();  // not known to CUDA: plain host memory
+    else if (at.type == cudaMemoryTypeDevice)
+        return;
     static const int64_t step = std::max<int64_t>(1, (int64_t)sysconf(_SC_PAGESIZE) / (int64_t)sizeof(double));
     volatile double* v = p;
     for (int64_t k = 0; k < count; k += step) v[k] = 0.0;
