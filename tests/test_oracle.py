@@ -147,6 +147,32 @@ def test_oracle_hierarchy_matches_reference(golden, orc) -> None:
         assert np.array_equal(L["s"][1:], arrays[f"h13_l{lvl}_s"][1:])
 
 
+def test_faces_once_builder_equals_reference_level(orc) -> None:
+    """The batched engine's fine-level builder computes each harmonic face
+    once and takes a cell's west/south faces from its neighbours' east/north
+    faces, then sums e + w + n + s in the reference's order. Bit-identity with
+    the reference level (level.hpp:57, :79-97) rests on harmonic(x, y) =
+    (2x)y/(x+y) being symmetric in IEEE arithmetic; numpy evaluates the same
+    operations in the same order, so this pins that claim on the CPU."""
+    rng = np.random.default_rng(5)
+    for n in (1, 2, 7, 16, 33):
+        for a in (np.exp(rng.normal(0.0, 3.0, (n, n))), np.where(rng.random((n, n)) < 0.5, 1e3, 1e-3)):
+            e, nf = a.copy(), a.copy()  # boundary faces: the cell's own permeability
+            e[:, :-1] = 2.0 * a[:, :-1] * a[:, 1:] / (a[:, :-1] + a[:, 1:])
+            nf[:-1, :] = 2.0 * a[:-1, :] * a[1:, :] / (a[:-1, :] + a[1:, :])
+            w, s = a.copy(), a.copy()
+            w[:, 1:] = e[:, :-1]
+            s[1:, :] = nf[:-1, :]
+            d = e + w + nf + s
+            L = orc.hierarchy(a)[0]
+            assert np.array_equal(L["diag"], d), n
+            assert np.array_equal(L["inv_diag"], 1.0 / d), n
+            assert np.array_equal(L["e"][:, : n - 1], e[:, : n - 1]), n
+            assert np.array_equal(L["w"][:, 1:], w[:, 1:]), n
+            assert np.array_equal(L["n"][: n - 1], nf[: n - 1]), n
+            assert np.array_equal(L["s"][1:], s[1:]), n
+
+
 def test_oracle_galerkin_identity(orc) -> None:
     """coarsen() == P^T A P entry-wise (reference tests/cpp/test_core.cpp:132-163)."""
     rng = np.random.default_rng(8)
