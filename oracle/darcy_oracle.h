@@ -3,7 +3,7 @@
  *
  * A plain-C restatement of the reference algorithm (darcy-cpp v1.0.0,
  * include/darcy/{level,multigrid,solver,blas}.hpp and src/bindings.cpp), used by
- * the tests as the parity checker and by bench.py as the timed CPU baseline.
+ * the tests as the parity reference and by bench.py as the timed CPU baseline.
  * The GPU library never links, loads or calls this code.
  *
  * Parity pin: tests/test_oracle.py checks this restatement against golden
@@ -50,7 +50,7 @@ int oracle_solve(const double* a, const double* f, int64_t n, const oracle_optio
                  double* history, oracle_result* res, char* err, int err_len);
 
 /* Warm-started variant: PCG from u0 instead of 0 (same stopping test,
- * ||r|| / ||b|| < tol with r = b - A u0). Not in the reference; used to judge
+ * ||r|| / ||b|| < tol with r = b - A u0). Not in the reference; used to assess
  * the learned warm start. */
 int oracle_solve_x0(const double* a, const double* f, const double* u0, int64_t n,
                     const oracle_options* opt, double* u, oracle_result* res, char* err, int err_len);
