@@ -208,9 +208,11 @@ PYBIND11_MODULE(_core, m) {
             res.device_ms = st.device_ms;
             return res;
         },
-        py::arg("a"), py::arg("f") = 1.0, py::kw_only(), py::arg("tol") = 1e-10, py::arg("max_iter") = 10000,
+        // the reference's arguments positional-or-keyword as in its binding
+        // (src/bindings.cpp:135-137); the additions keyword-only
+        py::arg("a"), py::arg("f") = 1.0, py::arg("tol") = 1e-10, py::arg("max_iter") = 10000,
         py::arg("preconditioner") = "multigrid", py::arg("pre_sweeps") = 1, py::arg("post_sweeps") = 1,
-        py::arg("cycle_index") = 2, py::arg("record_history") = false, py::arg("form") = "fp64",
+        py::arg("cycle_index") = 2, py::arg("record_history") = false, py::kw_only(), py::arg("form") = "fp64",
         py::arg("x0") = py::none(), "Solve -div(a grad u) = f with homogeneous Dirichlet boundary conditions.");
 
     m.def(
@@ -244,10 +246,11 @@ PYBIND11_MODULE(_core, m) {
             }
             return py::make_tuple(out, int64_array(iters), double_array(res), bool_array(conv));
         },
-        py::arg("a"), py::arg("f") = 1.0, py::kw_only(), py::arg("tol") = 1e-10, py::arg("max_iter") = 10000,
+        // as the reference's binding (src/bindings.cpp:194-196); the additions keyword-only
+        py::arg("a"), py::arg("f") = 1.0, py::arg("tol") = 1e-10, py::arg("max_iter") = 10000,
         py::arg("preconditioner") = "multigrid", py::arg("pre_sweeps") = 1, py::arg("post_sweeps") = 1,
-        py::arg("cycle_index") = 2, py::arg("threads") = 0, py::arg("form") = "fp64", py::arg("x0") = py::none(),
-        "Solve a batch of independent Darcy problems, one GPU launch for the whole batch.");
+        py::arg("cycle_index") = 2, py::arg("threads") = 0, py::kw_only(), py::arg("form") = "fp64",
+        py::arg("x0") = py::none(), "Solve a batch of independent Darcy problems, one GPU launch for the whole batch.");
 
     m.def(
         "solve_batch_uneven",
@@ -369,8 +372,9 @@ PYBIND11_MODULE(_core, m) {
             check(rc);
             return z;
         },
-        py::arg("a"), py::arg("r"), py::kw_only(), py::arg("pre_sweeps") = 1, py::arg("post_sweeps") = 1,
-        py::arg("cycle_index") = 2, py::arg("form") = "fp64",
+        // as the reference's binding (src/bindings.cpp:242-243); form keyword-only
+        py::arg("a"), py::arg("r"), py::arg("pre_sweeps") = 1, py::arg("post_sweeps") = 1,
+        py::arg("cycle_index") = 2, py::kw_only(), py::arg("form") = "fp64",
         "Apply one multigrid cycle to r from a zero initial guess, on the GPU.");
 
     m.def(

@@ -93,3 +93,67 @@ def test_fields_are_exported(built) -> None:
         darcy.two_phase_permeability(np.zeros((8, 8)), hi=1.0, lo=-1.0)
     with pytest.raises(ValueError):
         darcy.gaussian_random_field(0)
+
+
+# The reference binding's argument lists (src/bindings.cpp:135-137, :194-196,
+# :215, :242-243, :258): names and defaults, positional-or-keyword. Arguments
+# this engine adds (form, x0) come after them, keyword-only.
+REFERENCE_ARGS = {
+    "solve": [("a", None), ("f", "1.0"), ("tol", "1e-10"), ("max_iter", "10000"),
+              ("preconditioner", "'multigrid'"), ("pre_sweeps", "1"), ("post_sweeps", "1"),
+              ("cycle_index", "2"), ("record_history", "False")],
+    "solve_batch": [("a", None), ("f", "1.0"), ("tol", "1e-10"), ("max_iter", "10000"),
+                    ("preconditioner", "'multigrid'"), ("pre_sweeps", "1"), ("post_sweeps", "1"),
+                    ("cycle_index", "2"), ("threads", "0")],
+    "apply_operator": [("a", None), ("x", None)],
+    "apply_preconditioner": [("a", None), ("r", None), ("pre_sweeps", "1"), ("post_sweeps", "1"),
+                             ("cycle_index", "2")],
+    "set_num_threads": [("threads", None)],
+    "num_threads": [],
+    "has_openmp": [],
+}
+
+
+def _signature(fn) -> tuple[list[tuple[str, str | None]], list[str]]:
+    """(positional-or-keyword (name, default) pairs, keyword-only names) from
+    the first line of a pybind11 docstring."""
+    line = fn.__doc__.splitlines()[0]
+    inner = line[line.index("(") + 1: line.rindex(")")]
+    parts, depth, cur = [], 0, ""
+    for ch in inner:  # split at commas outside brackets
+        depth += ch == "["
+        depth -= ch == "]"
+        if ch == "," and depth == 0:
+            parts.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        parts.append(cur.strip())
+    positional, keyword, kw = [], [], False
+    for p in parts:
+        if p == "*":
+            kw = True
+            continue
+        name = p.split(":")[0].strip()
+        default = p.split(" = ", 1)[1].strip() if " = " in p else None
+        (keyword if kw else positional).append(name if kw else (name, default))
+    return positional, keyword
+
+
+@pytest.mark.parametrize("name", sorted(REFERENCE_ARGS))
+def test_core_signatures_match_the_reference_binding(built, name: str) -> None:
+    from darcy_cpp_gb300 import _core
+
+    positional, keyword = _signature(getattr(_core, name))
+    assert positional == REFERENCE_ARGS[name]
+    assert set(keyword) <= {"form", "x0"}
+
+
+def test_core_module_attributes(built) -> None:
+    from darcy_cpp_gb300 import _core
+
+    assert issubclass(_core.InvalidInput, ValueError)
+    assert isinstance(_core.__version__, str) and isinstance(_core.__compiler__, str)
+    for field in ("u", "iterations", "residual", "converged", "levels", "history"):
+        assert hasattr(_core.SolveResult, field)
