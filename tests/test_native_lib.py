@@ -157,3 +157,36 @@ def test_core_module_attributes(built) -> None:
     assert isinstance(_core.__version__, str) and isinstance(_core.__compiler__, str)
     for field in ("u", "iterations", "residual", "converged", "levels", "history"):
         assert hasattr(_core.SolveResult, field)
+
+
+# python/darcy/__init__.py:119-281: the package functions' positional
+# arguments, keyword-only arguments and defaults (tol defaults to 1e-10).
+PACKAGE_ARGS = {
+    "solve": (["a", "f"], {"f": 1.0, "tol": 1e-10, "max_iter": 10000, "preconditioner": "multigrid",
+                           "pre_sweeps": 1, "post_sweeps": 1, "cycle_index": 2, "record_history": False}),
+    "solve_batch": (["a", "f"], {"f": 1.0, "tol": 1e-10, "max_iter": 10000, "preconditioner": "multigrid",
+                                 "pre_sweeps": 1, "post_sweeps": 1, "cycle_index": 2, "threads": 0}),
+    "apply_operator": (["a", "x"], {}),
+    "apply_preconditioner": (["a", "r"], {"pre_sweeps": 1, "post_sweeps": 1, "cycle_index": 2}),
+    "num_threads": ([], {}),
+    "set_num_threads": (["threads"], {}),
+    "has_openmp": ([], {}),
+    "build_info": ([], {}),
+}
+
+
+@pytest.mark.parametrize("name", sorted(PACKAGE_ARGS))
+def test_package_signatures_match_the_reference(built, name: str) -> None:
+    import inspect
+
+    import darcy_cpp_gb300 as darcy
+
+    params = inspect.signature(getattr(darcy, name)).parameters.values()
+    positional = [p.name for p in params if p.kind == p.POSITIONAL_OR_KEYWORD]
+    defaults = {p.name: p.default for p in params if p.default is not p.empty}
+    want_pos, want_defaults = PACKAGE_ARGS[name]
+    assert positional == want_pos
+    extra = {k: v for k, v in defaults.items() if k not in want_defaults}
+    assert {k: v for k, v in defaults.items() if k in want_defaults} == want_defaults
+    assert set(extra) <= {"form", "x0"}
+    assert all(p.kind == p.KEYWORD_ONLY for p in params if p.name in extra)
