@@ -159,7 +159,7 @@ def test_core_module_attributes(built) -> None:
         assert hasattr(_core.SolveResult, field)
 
 
-# python/darcy/__init__.py:119-281: the package functions' positional
+# python/darcy/__init__.py:119-278: the package functions' positional
 # arguments, keyword-only arguments and defaults (tol defaults to 1e-10).
 PACKAGE_ARGS = {
     "solve": (["a", "f"], {"f": 1.0, "tol": 1e-10, "max_iter": 10000, "preconditioner": "multigrid",
