@@ -190,3 +190,23 @@ def test_package_signatures_match_the_reference(built, name: str) -> None:
     assert {k: v for k, v in defaults.items() if k in want_defaults} == want_defaults
     assert set(extra) <= {"form", "x0"}
     assert all(p.kind == p.KEYWORD_ONLY for p in params if p.name in extra)
+
+
+def test_result_classes_keep_the_reference_fields(built) -> None:
+    """python/darcy/__init__.py:63-114: frozen dataclasses with these fields in
+    this order; fields added here come last and have defaults, so code that
+    builds a result positionally or reads these fields works unchanged."""
+    import dataclasses
+
+    import darcy_cpp_gb300 as darcy
+
+    for cls, want in ((darcy.SolveResult, ["u", "iterations", "residual", "converged", "levels", "history"]),
+                      (darcy.BatchResult, ["u", "iterations", "residuals", "converged"])):
+        fields = dataclasses.fields(cls)
+        assert [f.name for f in fields][: len(want)] == want
+        assert cls.__dataclass_params__.frozen
+        for f in fields[len(want):]:
+            assert f.default is not dataclasses.MISSING or f.default_factory is not dataclasses.MISSING
+    r = darcy.BatchResult(u=np.zeros((2, 1, 1)), iterations=np.array([1, 2]), residuals=np.zeros(2),
+                          converged=np.array([True, False]))
+    assert r.all_converged is False
