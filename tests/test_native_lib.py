@@ -210,3 +210,13 @@ def test_result_classes_keep_the_reference_fields(built) -> None:
     r = darcy.BatchResult(u=np.zeros((2, 1, 1)), iterations=np.array([1, 2]), residuals=np.zeros(2),
                           converged=np.array([True, False]))
     assert r.all_converged is False
+
+
+def test_package_exports_every_reference_name(built) -> None:
+    """python/darcy/__init__.py:38-52 (__all__): every name is exported here too."""
+    import darcy_cpp_gb300 as darcy
+
+    for name in ("BatchResult", "SolveResult", "__version__", "apply_operator", "apply_preconditioner",
+                 "build_info", "gaussian_random_field", "has_openmp", "num_threads", "set_num_threads",
+                 "solve", "solve_batch", "two_phase_permeability"):
+        assert name in darcy.__all__ and hasattr(darcy, name), name
