@@ -6,7 +6,7 @@ OpenMP structure. This module loads it through ctypes. Only the tests,
 ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import it; the GPU
 package never does.
 
-When ``oracle/_ref/libdarcy_ref.so`` exists (built by ``oracle/build_ref.sh``
+When ``oracle/_ref/libdarcy_ref.so`` exists (built by ``oracle/build_ref.py``
 from the reference's own headers, only possible where the reference checkout
 is present) the ``ref_*`` helpers run the reference itself.
 """

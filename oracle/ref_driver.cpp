@@ -1,6 +1,7 @@
 // C-ABI shim over the REFERENCE's own headers (darcy-cpp v1.0.0,
-// include/darcy/*.hpp), compiled from where they lie by oracle/build_ref.sh
-// into oracle/_ref/ (never committed). Test infrastructure only: it lets the
+// include/darcy/*.hpp), compiled by oracle/build_ref.py from the checkout (or
+// from the unmodified copies it stages in baseline/_ref/_src for a machine
+// without one) into oracle/_ref/ (never committed). Test infrastructure only: it lets the
 // golden-vector script and the oracle tests run the reference itself, so the
 // C restatement in darcy_oracle.c is pinned against the real thing.
 #include <cstdint>

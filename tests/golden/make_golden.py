@@ -4,11 +4,12 @@ Everything here comes from the reference itself:
   * fields from the reference's own generator (python/darcy/fields.py), loaded
     by file path from the checkout;
   * solver outputs from the reference's own C++ headers, compiled by
-    oracle/build_ref.sh into oracle/_ref/libdarcy_ref.so and run with ONE
+    oracle/build_ref.py into oracle/_ref/libdarcy_ref.so and run with ONE
     OpenMP thread so reductions have a fixed order.
 
 Output: tests/golden/golden.npz (arrays) and tests/golden/golden.json (scalars).
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py [--ref PATH]   (default: $DARCY_REFERENCE, else
+        the checkout location oracle/build_ref.py names)
 """
 
 from __future__ import annotations
@@ -41,10 +42,15 @@ def sha(a: np.ndarray) -> str:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", type=Path, default=Path("/root/reference"))
+    import os
+
+    from oracle.build_ref import DEFAULT_REF
+
+    ap.add_argument("--ref", type=Path, default=Path(os.environ.get("DARCY_REFERENCE", DEFAULT_REF)))
     args = ap.parse_args()
     if not oracle.have_ref():
-        subprocess_rc = __import__("subprocess").run(["sh", str(ROOT / "oracle" / "build_ref.sh")]).returncode
+        subprocess_rc = __import__("subprocess").run(
+            [sys.executable, str(ROOT / "oracle" / "build_ref.py"), "--ref", str(args.ref)]).returncode
         if subprocess_rc or not oracle.have_ref():
             raise SystemExit("oracle/_ref/libdarcy_ref.so could not be built")
     oracle.ref_set_threads(1)

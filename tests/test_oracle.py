@@ -1,7 +1,7 @@
 """Pin the CPU oracle against the reference's own outputs (no GPU needed).
 
 The golden vectors were produced by the reference itself (its headers compiled
-by oracle/build_ref.sh, one OpenMP thread) and its field generator; see
+by oracle/build_ref.py, one OpenMP thread) and its field generator; see
 tests/golden/make_golden.py. Every GPU parity test compares against the
 oracle, so it must reproduce them exactly.
 """
