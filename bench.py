@@ -8,20 +8,38 @@ chosen form -- the FP32 cycle inside FP64 CG, the 8 problems as one batch
 (concurrent grid-engine solves) -- with the inputs already resident in HBM;
 `plain_fp64` is the drop-in FP64 solve, one problem per call, on the same
 fields; `e2e` is the chosen form through the package API from host arrays.
-The split of the gain (batched FP64, unbatched mixed, the single seed-1
-solve) is reported beside it, and the 64 x 64 batched solves/s (the other
-half of the metric), both forms, through the batched engine.
+`value` and `e2e` are both the mean over the timed steps. The split of the
+gain (batched FP64, unbatched mixed) and the seed-1 field solved alone are
+reported beside it, and after the headline:
+
+* `batch64`: 4096 problems of 64 x 64 (seeds 0..4095, {12, 3}), solves/s of
+  both forms and of the learned warm start (the other half of the metric);
+* `uneven4096`: 4096 problems with sides drawn from {32, ..., 256} per seed;
+* `combined`: 16384 problems of 128 x 128 plus 64 of 512 x 512 at contrast
+  1e4, with the warm-start network retrained at 128 x 128;
+* `cpu_baseline`: the reference itself on the host cores (bounded samples of
+  the same workloads).
+
+The compact figures of every workload are repeated as the last key
+(`summary`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --profile {solve,batch,net,kernels} [--n N] [--form F] [--reps R] ...
 
-`--impl reference` times the CPU oracle (the reference algorithm restated in
-C with the reference's OpenMP structure) on all host cores for the same
-workload. Data: synthetic fields from the reference's generator construction.
+`--impl reference` times the reference itself -- its own Python package and
+C++ extension (baseline/_ref, installed and compiled by oracle/build_ref.py)
+through its public API (`darcy.solve`, `darcy.solve_batch`) on all host cores
+-- or, where that package cannot be imported, the oracle (the reference
+algorithm restated in C with its OpenMP structure). It never imports this
+repository's package. `--profile` runs one workload a few times for a kernel
+profiler to watch (see profile()). Data: synthetic fields from the
+reference's generator construction.
 """
 
 from __future__ import annotations
 
 import argparse
+import importlib.util
 import json
 import os
 import statistics
@@ -48,17 +66,77 @@ TOL = 1e-10
 LEARN_TRAIN_SEEDS = range(10000, 30000)
 LEARN_EVAL_SEEDS = range(30000, 32000)
 LEARN_EPOCHS = 4
+# uneven batch: 4096 problems, side drawn per seed from these, {12, 3}
+UNEVEN_SIDES = [32, 48, 64, 96, 128, 192, 256]
+UNEVEN_COUNT = 4096
+# combined workload: 16384 x 128^2 (seeds 0..16383) + 64 x 512^2 (seeds
+# 100000..100063), a in {1e2, 1e-2}; its network is retrained at 128 x 128
+COMB_SMALL, COMB_SMALL_N, COMB_BIG, COMB_BIG_N, COMB_HI, COMB_LO = 16384, 128, 64, 512, 1e2, 1e-2
+COMB_BIG_SEED0 = 100000
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
 
+# ---------------------------------------------------------------- fields
+
+_FIELDS = None
+
+
+def fields_module():
+    """The field generator (darcy_cpp_gb300/fields.py, the reference
+    generator's construction) loaded by path: the reference arm and the worker
+    processes must not import the package, which loads its CUDA extension."""
+    global _FIELDS
+    if _FIELDS is None:
+        spec = importlib.util.spec_from_file_location("darcy_bench_fields", ROOT / "darcy_cpp_gb300" / "fields.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        _FIELDS = mod
+    return _FIELDS
+
+
 def field(n: int, seed: int, hi: float, lo: float) -> np.ndarray:
-    from darcy_cpp_gb300.fields import gaussian_random_field, two_phase_permeability
+    F = fields_module()
+    return F.two_phase_permeability(F.gaussian_random_field(n, seed=seed), hi=hi, lo=lo)
 
-    return two_phase_permeability(gaussian_random_field(n, seed=seed), hi=hi, lo=lo)
+
+def _fields_chunk(specs: list[tuple[int, int, float, float]]) -> list[np.ndarray]:
+    return [field(*s) for s in specs]
 
 
-def small_batch(count: int) -> np.ndarray:
-    return np.stack([field(N_SMALL, s, 12.0, 3.0) for s in range(count)])
+class FieldPool:
+    """Host field generation on all cores: worker processes started with
+    `spawn` before the first GPU call, each loading the generator by path."""
+
+    def __init__(self) -> None:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+
+        workers = max(1, min(16, (os.cpu_count() or 1)))
+        self.pool = cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
+        self.workers = workers
+
+    def make(self, specs: list[tuple[int, int, float, float]]) -> list[np.ndarray]:
+        if not specs:
+            return []
+        step = max(1, (len(specs) + 4 * self.workers - 1) // (4 * self.workers))
+        chunks = [specs[i:i + step] for i in range(0, len(specs), step)]
+        out: list[np.ndarray] = []
+        for part in self.pool.map(_fields_chunk, chunks):
+            out.extend(part)
+        return out
+
+    def close(self) -> None:
+        self.pool.shutdown()
+
+
+def uneven_specs() -> list[tuple[int, int, float, float]]:
+    return [(UNEVEN_SIDES[int(np.random.default_rng(s).integers(len(UNEVEN_SIDES)))], s, 12.0, 3.0)
+            for s in range(UNEVEN_COUNT)]
+
+
+def combined_specs() -> list[tuple[int, int, float, float]]:
+    return ([(COMB_SMALL_N, s, COMB_HI, COMB_LO) for s in range(COMB_SMALL)]
+            + [(COMB_BIG_N, COMB_BIG_SEED0 + s, COMB_HI, COMB_LO) for s in range(COMB_BIG)])
 
 
 # ------------------------------------------------------------------ clocks
@@ -115,7 +193,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ------------------------------------------------------------- GPU (ours)
+# ------------------------------------------------------------- helpers
 
 def load_traffic(kernel: str, workload: str) -> float | None:
     """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
@@ -165,7 +243,189 @@ def job_solves_per_s(slowest_s: float, solves: int, world: int) -> float:
     return solves * world / slowest_s
 
 
+def best_of(fn, runs: int, flush=None):
+    """(min seconds, last result) of `runs` calls of fn(); the previous result
+    is dropped before each call, outside the timed region."""
+    import torch
+
+    times, res = [], None
+    for _ in range(runs):
+        res = None
+        if flush is not None:
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = fn()
+        times.append(time.perf_counter() - t0)
+    return min(times), res
+
+
+# ------------------------------------------------------ CPU (the reference)
+
+class CpuReference:
+    """The reference on the host cores: its own package from baseline/_ref
+    (`kind` "reference": darcy.solve / darcy.solve_batch, the unmodified
+    reference compiled for this machine by oracle/build_ref.py), else the
+    oracle's C restatement (`kind` "port"). All host cores, OpenMP."""
+
+    def __init__(self) -> None:
+        self.cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        self.ref = None
+        self.why = ""
+        base = ROOT / "baseline" / "_ref"
+        if (base / "darcy" / "__init__.py").exists():
+            sys.path.insert(0, str(base))
+            try:
+                import darcy  # the reference's own package
+
+                if Path(darcy.__file__).resolve().parent != (base / "darcy").resolve():
+                    raise ImportError(f"`darcy` resolved to {darcy.__file__}, not baseline/_ref")
+                self.ref = darcy
+                self.ref.set_num_threads(self.cores)
+            except ImportError as exc:
+                self.why = f"reference package not importable: {exc}"
+                self.ref = None
+        else:
+            self.why = "baseline/_ref not installed"
+        if self.ref is None:
+            import oracle
+
+            self.oracle = oracle
+            oracle.set_threads(self.cores)
+
+    @property
+    def kind(self) -> str:
+        return "reference" if self.ref is not None else "port"
+
+    def describe(self) -> str:
+        if self.ref is not None:
+            return (f"reference darcy-cpp {self.ref.__version__} ({self.ref.build_info().get('compiler')}, OpenMP, "
+                    f"{self.cores} threads) through darcy.solve / darcy.solve_batch")
+        return f"oracle C port (OpenMP, {self.cores} threads); {self.why}"
+
+    def solve(self, a: np.ndarray) -> int:
+        """One solve; returns its iteration count."""
+        if self.ref is not None:
+            return int(self.ref.solve(a, tol=TOL).iterations)
+        return int(self.oracle.solve(a, tol=TOL)["iterations"])
+
+    def solve_batch(self, batch: np.ndarray) -> np.ndarray:
+        if self.ref is not None:
+            return np.asarray(self.ref.solve_batch(batch, tol=TOL, threads=self.cores).iterations)
+        return np.asarray(self.oracle.solve_batch(batch, tol=TOL, threads=self.cores)["iterations"])
+
+    def solve_groups(self, arrays: list[np.ndarray]) -> float:
+        """Problems of several sides: one batch call per side (the reference's
+        solve_batch takes one side); returns the seconds taken."""
+        by: dict[int, list[np.ndarray]] = {}
+        for x in arrays:
+            by.setdefault(x.shape[0], []).append(x)
+        t0 = time.perf_counter()
+        for n in sorted(by):
+            self.solve_batch(np.stack(by[n]))
+        return time.perf_counter() - t0
+
+
+def cpu_samples(cpu: CpuReference, bigs: list[np.ndarray], batch64: np.ndarray, uneven: list[np.ndarray],
+                comb: list[np.ndarray]) -> dict:
+    """Bounded samples of each workload on the host cores (~20-30 s)."""
+    t0 = time.perf_counter()
+    its = [cpu.solve(a) for a in bigs]
+    per_big = (time.perf_counter() - t0) / len(bigs)
+    b = batch64[:1024]
+    t0 = time.perf_counter()
+    cpu.solve_batch(b)
+    s64 = len(b) / (time.perf_counter() - t0)
+    sec_uneven = cpu.solve_groups(uneven)
+    small = np.stack(comb[:512])
+    t0 = time.perf_counter()
+    cpu.solve_batch(small)
+    ms128 = (time.perf_counter() - t0) * 1e3 / len(small)
+    big = np.stack(comb[COMB_SMALL:COMB_SMALL + 16])
+    t0 = time.perf_counter()
+    cpu.solve_batch(big)
+    ms512 = (time.perf_counter() - t0) * 1e3 / len(big)
+    comb_s = (COMB_SMALL * ms128 + COMB_BIG * ms512) * 1e-3
+    return {"value": round(per_big * 1e3, 2), "unit": "ms/solve", "cores": cpu.cores, "kind": cpu.kind,
+            "impl": cpu.describe(),
+            "sample": (f"1024x1024: the 8 fields once each ({sum(its)} iterations), mean; 64x64: batch of 1024; "
+                       f"uneven: all {len(uneven)} problems, one batch per side; combined: 512 of the 128x128 and "
+                       f"16 of the 512x512 problems, total extrapolated per size"),
+            "batch64_solves_per_s": round(s64, 1),
+            "uneven4096_solves_per_s": round(len(uneven) / sec_uneven, 1),
+            "combined": {"ms_per_solve_128": round(ms128, 3), "ms_per_solve_512": round(ms512, 2),
+                         "solves_per_s": round((COMB_SMALL + COMB_BIG) / comb_s, 1)}}
+
+
+def run_reference(args, rank: int, world: int) -> dict | None:
+    """The reference arm: the reference itself on the host cores, same
+    workload, metric and step count as the GPU arm (rank 0 only)."""
+    if rank != 0:
+        return None
+    cpu = CpuReference()
+    if cpu.ref is not None:
+        F = cpu.ref  # the reference's own field generator
+
+        def gen(n, s, hi, lo):
+            return F.two_phase_permeability(F.gaussian_random_field(n, seed=s), hi=hi, lo=lo)
+    else:
+        gen = field
+    bigs = [gen(N_BIG, q, HI_BIG, LO_BIG) for q in SEEDS_BIG]
+    for q in range(args.warmup):  # a warm-up step: one field
+        cpu.solve(bigs[q % len(bigs)])
+    times, its = [], []
+    for _ in range(args.steps):  # a step: the 8 fields, one solve each
+        t0 = time.perf_counter()
+        its = [cpu.solve(a) for a in bigs]
+        times.append((time.perf_counter() - t0) * 1e3 / len(bigs))
+    batch = np.stack([gen(N_SMALL, s, 12.0, 3.0) for s in range(1024)])
+    cpu.solve_batch(batch[:64])
+    t0 = time.perf_counter()
+    cpu.solve_batch(batch)
+    bsec = time.perf_counter() - t0
+    value = sum(times) / len(times)
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "ms/solve",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(value * len(bigs), 2),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: two-phase GRF fields (reference generator construction), seeded",
+        "config": {"workload": WORKLOAD, "form": f"the reference on the host CPU: {cpu.describe()}, one solve per call",
+                   "warmup_step": "one field"},
+        "iterations": its,
+        "batch64": {"metric": "64x64 solves/s (1024 problems, seeds 0..1023, {12,3}), darcy.solve_batch",
+                    "value": round(1024 / bsec, 1), "unit": "solves/s"},
+        "cpu_baseline": {"value": round(value, 2), "unit": "ms/solve", "cores": cpu.cores, "kind": cpu.kind,
+                         "sample": f"{args.steps} step(s) of the 8-field 1024x1024 workload, mean per solve"},
+        "e2e": {"value": round(value, 2), "unit": "ms/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ------------------------------------------------------------- GPU (ours)
+
 def run_ours(args, rank: int, world: int) -> dict | None:
+    # host fields first: the worker processes start before any GPU call
+    pool = FieldPool()
+    try:
+        bigs = np.stack(pool.make([(N_BIG, q, HI_BIG, LO_BIG) for q in SEEDS_BIG]))
+        batch = np.stack(pool.make([(N_SMALL, s, 12.0, 3.0) for s in range(BATCH_SMALL)]))
+        uneven = pool.make(uneven_specs())
+        comb = pool.make(combined_specs())
+        learn64 = (np.stack(pool.make([(N_SMALL, s, 12.0, 3.0) for s in LEARN_TRAIN_SEEDS])),
+                   np.stack(pool.make([(N_SMALL, s, 12.0, 3.0) for s in LEARN_EVAL_SEEDS])))
+        learn128 = (np.stack(pool.make([(COMB_SMALL_N, s, COMB_HI, COMB_LO) for s in LEARN_TRAIN_SEEDS])),
+                    np.stack(pool.make([(COMB_SMALL_N, s, COMB_HI, COMB_LO) for s in LEARN_EVAL_SEEDS])))
+    finally:
+        pool.close()
+
     import torch
 
     import darcy_cpp_gb300 as darcy
@@ -176,9 +436,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     ctx = capi.Context(dev)
     stream = torch.cuda.current_stream()
 
-    a_big = field(N_BIG, SEED_BIG, HI_BIG, LO_BIG)
-    bigs = np.stack([field(N_BIG, q, HI_BIG, LO_BIG) for q in SEEDS_BIG])
-    nb, m = len(SEEDS_BIG), a_big.size
+    nb, m = len(SEEDS_BIG), N_BIG * N_BIG
     d_a = torch.from_numpy(bigs).to(f"cuda:{dev}")
     d_u = torch.empty_like(d_a)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -216,7 +474,11 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         res = [darcy.solve(bigs[q], tol=TOL, form=form) for q in range(nb)]
         return (time.perf_counter() - t0) * 1e3, res
 
-    out: dict = {}
+    def launches_of(name: str, r) -> int:
+        if isinstance(r, dict):
+            return int(r["kernel_launches"])
+        return int(sum(st.kernel_launches for st in r))
+
     # warm-up: graph capture, plan allocation, clocks
     for _ in range(max(args.warmup, 3)):
         for form in ("mixed", "fp64"):
@@ -230,13 +492,14 @@ def run_ours(args, rank: int, world: int) -> dict | None:
 
     with ClockSampler(dev) as clocks:
         arms = {"mixed_batch": [], "fp64_serial": [], "fp64_batch": [], "mixed_serial": []}
-        res = {}
+        res, launches = {}, 0
         for _ in range(args.steps):
             for name in arms:
                 form, how = name.split("_")
                 ms, r = (device_batch if how == "batch" else device_serial)(form)
                 arms[name].append(ms)
                 res[name] = r
+                launches += launches_of(name, r)
         e2e = {"mixed_batch": [], "fp64_serial": []}
         e2e_res = {}
         for _ in range(args.steps):
@@ -246,23 +509,14 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             ms, r = e2e_serial("fp64")
             e2e["fp64_serial"].append(ms)
             e2e_res["fp64_serial"] = r
-        # 64 x 64 batch (the solves/s half of the metric)
-        batch = small_batch(BATCH_SMALL)
+        torch.cuda.synchronize()
+
+        # ---- 64 x 64 batch (the solves/s half of the metric)
         for form in ("mixed", "fp64"):  # launch shape tuned for the full batch, untimed
             darcy.solve_batch(batch, tol=TOL, form=form)
-        bt = {}
-        for form in ("mixed", "fp64"):
-            runs = []
-            br = None
-            for _ in range(max(3, args.steps)):  # best of several: one 25-45 ms run is noisy
-                br = None  # the previous result is freed outside the timed call
-                flush.zero_()
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                br = darcy.solve_batch(batch, tol=TOL, form=form)
-                runs.append(time.perf_counter() - t0)
-            bt[form] = (min(runs), br)
-        # the same batch resident in HBM (device pointers, no host copies)
+        runs64 = max(3, min(args.steps, 5))  # best of several: one 25-45 ms run is noisy
+        bt = {form: best_of(lambda form=form: darcy.solve_batch(batch, tol=TOL, form=form), runs64, flush)
+              for form in ("mixed", "fp64")}
         d_batch = torch.from_numpy(batch).to(f"cuda:{dev}")
         d_ub = torch.empty_like(d_batch)
         bdev = {}
@@ -270,22 +524,25 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             ctx.solve_batch_device(d_batch.data_ptr(), BATCH_SMALL, N_SMALL, d_ub.data_ptr(), stream.cuda_stream,
                                    tol=TOL, form=form)  # tune
             runs = []
-            for _ in range(max(3, args.steps)):  # best of several: one 25-45 ms run is noisy
-                flush.zero_()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                rr = ctx.solve_batch_device(d_batch.data_ptr(), BATCH_SMALL, N_SMALL, d_ub.data_ptr(),
-                                            stream.cuda_stream, tol=TOL, form=form)
-                e1.record(stream)
-                e1.synchronize()
-                runs.append(e0.elapsed_time(e1))
+            for _ in range(runs64):
+                ms, _r = timed(lambda form=form: ctx.solve_batch_device(
+                    d_batch.data_ptr(), BATCH_SMALL, N_SMALL, d_ub.data_ptr(), stream.cuda_stream, tol=TOL,
+                    form=form))
+                runs.append(ms)
             bdev[form] = min(runs)
-        learned = run_learned(batch, flush)
+        del d_batch, d_ub
+        learned = run_learned(batch, learn64, flush)
+
+        # ---- uneven batch and combined workload (end to end, host arrays)
+        uneven_res = run_uneven(uneven, flush)
+        comb_res = run_combined(comb, learn128, flush)
+    cpu = cpu_samples(CpuReference(), list(bigs), batch, uneven, comb)
+
     total_ms = {k: sum(v) for k, v in arms.items()}
     names = sorted(total_ms)
-    e2e_med = [statistics.median(e2e["mixed_batch"]), statistics.median(e2e["fp64_serial"])]
+    e2e_tot = [sum(e2e["mixed_batch"]), sum(e2e["fp64_serial"])]
     slowest = replica_max([total_ms[k] for k in names] + [bt["mixed"][0], bt["fp64"][0], bdev["mixed"],
-                                                          bdev["fp64"]] + e2e_med, world, f"cuda:{dev}")
+                                                          bdev["fp64"]] + e2e_tot, world, f"cuda:{dev}")
     total_ms = dict(zip(names, slowest[: len(names)]))
     bt_s = {"mixed": slowest[len(names)], "fp64": slowest[len(names) + 1]}
     bdev_ms = {"mixed": slowest[len(names) + 2], "fp64": slowest[len(names) + 3]}
@@ -297,7 +554,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     per_solve = {k: job_ms_per_solve(v, args.steps, nb, world) for k, v in total_ms.items()}
     ms_mixed = per_solve["mixed_batch"]
     ms_fp64 = per_solve["fp64_serial"]
-    e2e_mixed = job_ms_per_solve(e2e_slowest["mixed_batch"], 1, nb, world)
+    e2e_mixed = job_ms_per_solve(e2e_slowest["mixed_batch"], args.steps, nb, world)
+    e2e_fp64 = job_ms_per_solve(e2e_slowest["fp64_serial"], args.steps, nb, world)
     serial_m, serial_p = res["mixed_serial"], res["fp64_serial"]
     batch_m = res["mixed_batch"]
     it_m = [int(v) for v in batch_m["iterations"]]
@@ -305,28 +563,35 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     ref_us = [r.u for r in e2e_res["fp64_serial"]]
     mixed_err = float(max(np.linalg.norm(e2e_res["mixed_batch"].u[q] - ref_us[q]) / np.linalg.norm(ref_us[q])
                           for q in range(nb)))
-    single = {"workload": "the seed-1 field alone, one solve per call (library-timed, device buffers)",
-              "mixed": round(serial_m[0].device_ms, 3), "fp64": round(serial_p[0].device_ms, 3),
+    single = {"workload": "the seed-1 field alone, one solve per call (library-timed, device buffers, last step)",
+              "mixed_ms": round(serial_m[0].device_ms, 3), "fp64_ms": round(serial_p[0].device_ms, 3),
               "iterations": {"mixed": int(serial_m[0].iterations), "fp64": int(serial_p[0].iterations)},
               "fp64_over_mixed": round(serial_p[0].device_ms / serial_m[0].device_ms, 3)}
 
-    prof = ctx.profile_kernels(a_big, reps=20, tol=TOL, form="mixed")
-    for row in prof:
-        row["share_ms"] = row["avg_ms"] * row["launches_per_iteration"]
-    peaks = load_peaks()
-    dom = max(prof, key=lambda k: k["share_ms"])
-    achieved = dom["bytes"] / (dom["avg_ms"] * 1e-3) / 1e9
-    traffic = load_traffic(dom["name"], "1024x1024 mixed")
-    roofline = {"bound": "hbm", "kernel": dom["name"], "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
-                "traffic_source": "profiles/dram_traffic.md (ncu, cold L2, one launch)" if traffic else None,
-                "peak_source": peaks["source"], "avg_launch_us": round(dom["avg_ms"] * 1e3, 3),
-                "algorithmic_bytes_per_launch": dom["bytes"],
-                "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()} for p in prof]}
+    roofline = measure_roofline(ctx, bigs[0], serial_m[0])
 
-    cpu = run_cpu_baseline()
     bsm = job_solves_per_s(bt_s["mixed"], BATCH_SMALL, world)
     bsp = job_solves_per_s(bt_s["fp64"], BATCH_SMALL, world)
+    b64 = {"metric": "64x64 solves/s (4096 problems, seeds 0..4095, {12,3})",
+           "mixed": round(bsm, 1), "fp64": round(bsp, 1), "unit": "solves/s",
+           "chosen_vs_plain": round(bsm / bsp, 3),
+           "mean_iterations": {"mixed": float(bt["mixed"][1].iterations.mean()),
+                               "fp64": float(bt["fp64"][1].iterations.mean())},
+           "timing": f"end to end through darcy_cpp_gb300.solve_batch from host arrays, best of {runs64}",
+           "h2d_bytes": int(batch.nbytes), "d2h_bytes": int(batch.nbytes),
+           "device_resident": {"mixed": round(job_solves_per_s(bdev_ms["mixed"] * 1e-3, BATCH_SMALL, world), 1),
+                               "fp64": round(job_solves_per_s(bdev_ms["fp64"] * 1e-3, BATCH_SMALL, world), 1),
+                               "chosen_vs_plain": round(bdev_ms["fp64"] / bdev_ms["mixed"], 3),
+                               "unit": "solves/s", "timing": f"CUDA events, inputs in HBM, best of {runs64}"},
+           "mixed_learned": learned["solves_per_s"],
+           "learned_vs_plain": round(learned["solves_per_s"] / bsp, 3),
+           "cpu_reference": cpu["batch64_solves_per_s"]}
+    spread = {"value_ms_per_step": {"mean": round(statistics.mean(arms["mixed_batch"]), 3),
+                                    "median": round(statistics.median(arms["mixed_batch"]), 3),
+                                    "min": round(min(arms["mixed_batch"]), 3)},
+              "e2e_ms_per_step": {"mean": round(statistics.mean(e2e["mixed_batch"]), 3),
+                                  "median": round(statistics.median(e2e["mixed_batch"]), 3),
+                                  "min": round(min(e2e["mixed_batch"]), 3)}}
     line = {
         "metric": METRIC,
         "value": round(ms_mixed, 3),
@@ -341,56 +606,92 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "dtype": "f64 CG + f32 cycle",
         "data": "synthetic: two-phase GRF fields (reference generator construction), seeded",
         "config": {"workload": WORKLOAD, "form": "mixed (FP32 W-cycle inside FP64 CG), batched",
-                   "l2": "flushed between timed steps", "parallelism": f"replicas x{world}"},
+                   "l2": "flushed between timed steps", "parallelism": f"replicas x{world}",
+                   "statistic": "value and e2e: mean over the timed steps"},
         "iterations": {"mixed": it_m, "fp64": it_p},
         "mixed_vs_fp64_rel_l2_max": mixed_err,
         "plain_fp64": {"value": round(ms_fp64, 3), "unit": "ms/solve", "how": "one solve per call, FP64",
-                       "e2e": round(job_ms_per_solve(e2e_slowest["fp64_serial"], 1, nb, world), 3)},
+                       "e2e": round(e2e_fp64, 3)},
         "chosen_vs_plain": round(ms_fp64 / ms_mixed, 3),
         "split": {"fp64_batched": round(per_solve["fp64_batch"], 3),
-                  "mixed_one_per_call": round(per_solve["mixed_serial"], 3), "unit": "ms/solve",
-                  "single_seed1": single},
-        "batch64": {"metric": "64x64 solves/s (4096 problems, seeds 0..4095, {12,3})",
-                    "mixed": round(bsm, 1), "fp64": round(bsp, 1), "unit": "solves/s",
-                    "chosen_vs_plain": round(bsm / bsp, 3),
-                    "mean_iterations": float(bt["mixed"][1].iterations.mean()),
-                    "e2e": True, "h2d_bytes": int(batch.nbytes), "d2h_bytes": int(batch.nbytes),
-                    "device_resident": {"mixed": round(job_solves_per_s(bdev_ms["mixed"] * 1e-3, BATCH_SMALL, world), 1),
-                                        "fp64": round(job_solves_per_s(bdev_ms["fp64"] * 1e-3, BATCH_SMALL, world), 1),
-                                        "chosen_vs_plain": round(bdev_ms["fp64"] / bdev_ms["mixed"], 3),
-                                        "unit": "solves/s", "timing": "CUDA events, inputs in HBM"},
-                    "mixed_learned": learned["solves_per_s"],
-                    "learned_vs_plain": round(learned["solves_per_s"] / bsp, 3),
-                    "learned_mean_iterations": learned["mean_iterations"]},
-        "learned": learned,
+                  "mixed_one_per_call": round(per_solve["mixed_serial"], 3), "unit": "ms/solve"},
+        "spread": spread,
         "e2e": {"value": round(e2e_mixed, 3), "unit": "ms/solve", "h2d_bytes_per_step": int(8 * m * nb),
                 "d2h_bytes_per_step": int(8 * m * nb)},
-        "gpu_launches": int(batch_m["kernel_launches"]),
+        "gpu_launches": launches,
         "roofline": roofline,
+        "learned": learned,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
+        "single_seed1": single,
+        "batch64": b64,
+        "uneven4096": {**uneven_res, "cpu_reference_solves_per_s": cpu["uneven4096_solves_per_s"]},
+        "combined": {**comb_res, "cpu_reference": cpu["combined"]},
     }
+    line["summary"] = summary_of(line)
     return line
 
 
-def run_learned(batch: np.ndarray, flush) -> dict:
+def summary_of(line: dict) -> dict:
+    """The compact figures of every workload (the last key of the line)."""
+    b, u, c, s = line["batch64"], line["uneven4096"], line["combined"], line["single_seed1"]
+    return {
+        "1024_batch8_ms": {"chosen": line["value"], "plain_fp64": line["plain_fp64"]["value"],
+                           "ratio": line["chosen_vs_plain"], "e2e": line["e2e"]["value"]},
+        "1024_single_seed1_ms": {"mixed": s["mixed_ms"], "fp64": s["fp64_ms"], "ratio": s["fp64_over_mixed"]},
+        "64_batch_solves_per_s": {"mixed": b["mixed"], "fp64": b["fp64"], "ratio": b["chosen_vs_plain"],
+                                  "hbm_ratio": b["device_resident"]["chosen_vs_plain"],
+                                  "learned": b["mixed_learned"], "cpu": b["cpu_reference"]},
+        "uneven4096_solves_per_s": {"mixed": u["mixed"], "fp64": u["fp64"], "ratio": u["chosen_vs_plain"],
+                                    "cpu": u["cpu_reference_solves_per_s"]},
+        "combined_solves_per_s": {"mixed": c["mixed"]["solves_per_s"], "fp64": c["fp64"]["solves_per_s"],
+                                  "learned": c["learned"]["solves_per_s"], "cpu": c["cpu_reference"]["solves_per_s"]},
+        "roofline_frac": line["roofline"]["frac"],
+    }
+
+
+def measure_roofline(ctx, a_big: np.ndarray, single_stats) -> dict:
+    """Each kernel of one CG iteration of the seed-1 solve timed back to back
+    (CUDA events, dgpu_profile_kernels), weighted by its launches per
+    iteration; the dominant one against the measured HBM copy peak."""
+    prof = ctx.profile_kernels(a_big, reps=20, tol=TOL, form="mixed")
+    for row in prof:
+        row["share_ms"] = row["avg_ms"] * row["launches_per_iteration"]
+    peaks = load_peaks()
+    dom = max(prof, key=lambda k: k["share_ms"])
+    achieved = dom["bytes"] / (dom["avg_ms"] * 1e-3) / 1e9
+    traffic = load_traffic(dom["name"], "1024x1024 mixed")
+    per_it = single_stats.device_ms / max(1, single_stats.iterations)
+    covered = sum(r["share_ms"] for r in prof)
+    return {"bound": "hbm", "kernel": dom["name"], "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+            "traffic_source": "profiles/dram_traffic.md (ncu, one launch)" if traffic else None,
+            "peak_source": peaks["source"], "avg_launch_us": round(dom["avg_ms"] * 1e3, 3),
+            "algorithmic_bytes_per_launch": dom["bytes"],
+            "share_of_iteration": round(dom["share_ms"] / per_it, 4),
+            "kernels_cover": {"sum_of_shares_ms": round(covered, 4), "iteration_ms": round(per_it, 4),
+                              "fraction": round(covered / per_it, 3),
+                              "note": "shares from back-to-back launches of each kernel alone; the iteration "
+                                      "from the seed-1 mixed solve's device time / iterations"},
+            "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()} for p in prof]}
+
+
+def run_learned(batch: np.ndarray, pairs: tuple[np.ndarray, np.ndarray], flush) -> dict:
     """Trains the warm-start network on solver-generated 64 x 64 pairs, then
     times the batched mixed solve with the predicted start (prediction on the
     device, inside the timed call) and compares iterations on held-out fields."""
-    import torch
-
     import darcy_cpp_gb300 as darcy
     from darcy_cpp_gb300 import learn
 
+    a_tr, held = pairs
     t0 = time.perf_counter()
-    a_tr, u_tr = learn.generate_pairs(LEARN_TRAIN_SEEDS, N_SMALL)
+    u_tr = solve_pairs(a_tr, 1.0)
     gen_s = time.perf_counter() - t0
     net = learn.WarmStartNet(N_SMALL, seed=0)
-    steps = LEARN_EPOCHS * len(LEARN_TRAIN_SEEDS) // 256
+    steps = LEARN_EPOCHS * len(a_tr) // 256
     t0 = time.perf_counter()
     losses = net.fit(a_tr, u_tr, steps=steps, batch=256, lr=1e-3)
     train_s = time.perf_counter() - t0
-    held = learn.permeability_fields(LEARN_EVAL_SEEDS, N_SMALL)
     zero = darcy.solve_batch(held, tol=TOL, form="mixed")
     warm = learn.solve_batch_learned(net, held, tol=TOL, form="mixed")
     ref = darcy.solve_batch(held[:64], tol=TOL, form="fp64")
@@ -398,97 +699,160 @@ def run_learned(batch: np.ndarray, flush) -> dict:
     u0_err = float(np.mean([np.linalg.norm(u0[q] - ref.u[q]) / np.linalg.norm(ref.u[q]) for q in range(64)]))
     sol_err = float(max(np.linalg.norm(warm.u[q] - ref.u[q]) / np.linalg.norm(ref.u[q]) for q in range(64)))
     learn.solve_batch_learned(net, batch, tol=TOL, form="mixed")  # launch shape tuned, untimed
-    runs = []
-    r = None
-    for _ in range(3):
-        r = None  # the previous result is freed outside the timed call
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = learn.solve_batch_learned(net, batch, tol=TOL, form="mixed")
-        runs.append(time.perf_counter() - t0)
-    return {"solves_per_s": round(BATCH_SMALL / min(runs), 1), "mean_iterations": float(r.iterations.mean()),
+    sec, r = best_of(lambda: learn.solve_batch_learned(net, batch, tol=TOL, form="mixed"), 3, flush)
+    return {"solves_per_s": round(BATCH_SMALL / sec, 1), "mean_iterations": float(r.iterations.mean()),
             "all_converged": bool(r.all_converged),
             "heldout": {"seeds": f"{LEARN_EVAL_SEEDS.start}..{LEARN_EVAL_SEEDS.stop - 1}",
                         "mean_iterations_zero_start": float(zero.iterations.mean()),
                         "mean_iterations_learned_start": float(warm.iterations.mean()),
                         "u0_rel_l2_vs_solution": round(u0_err, 4),
                         "solution_rel_l2_vs_fp64": sol_err},
-            "training": {"pairs": len(LEARN_TRAIN_SEEDS), "pair_generation_s": round(gen_s, 2),
+            "training": {"pairs": len(a_tr), "pair_generation_s": round(gen_s, 2),
                          "steps": steps, "batch": 256, "lr": 1e-3, "seconds": round(train_s, 2),
                          "loss_first": float(losses[0]), "loss_last": float(np.mean(losses[-20:])),
                          "loss": "energy norm of u0 - u relative to u"},
             "net": net.handle.info()}
 
 
-# ------------------------------------------------------- CPU (the oracle)
+def solve_pairs(a: np.ndarray, f: float) -> np.ndarray:
+    """Training targets: the GPU solver's FP64 solutions of `a` (all must converge)."""
+    import darcy_cpp_gb300 as darcy
 
-def run_cpu_baseline() -> dict:
-    """The reference algorithm (oracle C port, OpenMP) on all host cores: the
-    8-field 1024 x 1024 workload once, and a 64 x 64 batch of 256."""
-    import oracle
+    u = np.empty_like(a)
+    for at in range(0, len(a), 8192):
+        r = darcy.solve_batch(a[at:at + 8192], f, tol=TOL, form="fp64")
+        if not r.all_converged:
+            raise RuntimeError("a training solve did not converge")
+        u[at:at + 8192] = r.u
+    return u
 
-    cores = oracle.cpu_count()
-    oracle.set_threads(cores)
-    bigs = [field(N_BIG, q, HI_BIG, LO_BIG) for q in SEEDS_BIG]
+
+def run_uneven(fields: list[np.ndarray], flush) -> dict:
+    """4096 problems of sides 32..256 in one call, both forms, end to end."""
+    import darcy_cpp_gb300 as darcy
+
+    out: dict = {"metric": f"solves/s, {len(fields)} problems, side per seed from {UNEVEN_SIDES}, {{12,3}}",
+                 "unit": "solves/s", "timing": "end to end through solve_batch_uneven from host arrays, best of 3"}
+    for form in ("mixed", "fp64"):
+        darcy.solve_batch_uneven(fields, tol=TOL, form=form)  # launch shape tuned, untimed
+        sec, r = best_of(lambda form=form: darcy.solve_batch_uneven(fields, tol=TOL, form=form), 3, flush)
+        out[form] = round(len(fields) / sec, 1)
+        out[f"{form}_mean_iterations"] = round(float(r.iterations.mean()), 3)
+        out[f"{form}_all_converged"] = bool(r.all_converged)
+    out["chosen_vs_plain"] = round(out["mixed"] / out["fp64"], 3)
+    return out
+
+
+def run_combined(fields: list[np.ndarray], pairs: tuple[np.ndarray, np.ndarray], flush) -> dict:
+    """16384 x 128^2 + 64 x 512^2 at contrast 1e4: both forms with a zero
+    start in one call each, then the mixed form with the warm start of a
+    network retrained at 128 x 128 on solver-generated pairs (the 128^2
+    problems from the predicted start, the 512^2 ones from zero)."""
+    import darcy_cpp_gb300 as darcy
+    from darcy_cpp_gb300 import learn
+
+    small, big = np.stack(fields[:COMB_SMALL]), fields[COMB_SMALL:]
+    total = len(fields)
+    out: dict = {"metric": f"{COMB_SMALL} x {COMB_SMALL_N}^2 + {COMB_BIG} x {COMB_BIG_N}^2, a in "
+                           f"{{{COMB_HI:g},{COMB_LO:g}}}: total solves/s and ms/solve per size",
+                 "timing": "end to end from host arrays, best of 2"}
+    for form in ("mixed", "fp64"):
+        darcy.solve_batch_uneven(fields, tol=TOL, form=form)  # launch shape tuned, untimed
+        sec, r = best_of(lambda form=form: darcy.solve_batch_uneven(fields, tol=TOL, form=form), 2, flush)
+        # per-size cost from each size alone (one call per size, same form)
+        s_small, _ = best_of(lambda form=form: darcy.solve_batch(small, tol=TOL, form=form), 1, flush)
+        s_big, _ = best_of(lambda form=form: darcy.solve_batch_uneven(big, tol=TOL, form=form), 1, flush)
+        out[form] = {"solves_per_s": round(total / sec, 1), "seconds": round(sec, 4),
+                     "mean_iterations_128": round(float(r.iterations[:COMB_SMALL].mean()), 3),
+                     "mean_iterations_512": round(float(r.iterations[COMB_SMALL:].mean()), 3),
+                     "all_converged": bool(r.all_converged),
+                     "ms_per_solve_128_alone": round(s_small * 1e3 / COMB_SMALL, 5),
+                     "ms_per_solve_512_alone": round(s_big * 1e3 / len(big), 3)}
+    # the network retrained at 128 x 128 on pairs from this contrast
+    a_tr, held = pairs
     t0 = time.perf_counter()
-    its = [oracle.solve(a, tol=TOL)["iterations"] for a in bigs]
-    per = (time.perf_counter() - t0) / len(bigs)
-    batch = small_batch(256)
+    u_tr = solve_pairs(a_tr, 1.0)
+    gen_s = time.perf_counter() - t0
+    net = learn.WarmStartNet(COMB_SMALL_N, seed=0)
+    steps = LEARN_EPOCHS * len(a_tr) // 256
     t0 = time.perf_counter()
-    oracle.solve_batch(batch, tol=TOL, threads=cores)
-    bsec = time.perf_counter() - t0
-    return {"value": round(per * 1e3, 2), "unit": "ms/solve", "cores": cores, "kind": "port",
-            "sample": f"the 8 fields of the 1024x1024 workload once each ({sum(its)} iterations), mean; "
-                      f"64x64 batch of 256: {256 / bsec:.1f} solves/s",
-            "batch64_solves_per_s": round(256 / bsec, 1)}
+    losses = net.fit(a_tr, u_tr, steps=steps, batch=256, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    zero = darcy.solve_batch(held, tol=TOL, form="mixed")
+    warm = learn.solve_batch_learned(net, held, tol=TOL, form="mixed")
+    learn.solve_batch_learned(net, small, tol=TOL, form="mixed")  # launch shape tuned, untimed
+
+    def learned_call():
+        w = learn.solve_batch_learned(net, small, tol=TOL, form="mixed")
+        z = darcy.solve_batch_uneven(big, tol=TOL, form="mixed")
+        return w, z
+
+    sec, (w, z) = best_of(learned_call, 2, flush)
+    out["learned"] = {"solves_per_s": round(total / sec, 1), "seconds": round(sec, 4),
+                      "how": "128^2 problems: solve_batch_learned (prediction on the device); 512^2: zero start; "
+                             "two calls",
+                      "mean_iterations_128": round(float(w.iterations.mean()), 3),
+                      "all_converged": bool(w.all_converged and z.all_converged),
+                      "heldout": {"seeds": f"{LEARN_EVAL_SEEDS.start}..{LEARN_EVAL_SEEDS.stop - 1}",
+                                  "mean_iterations_zero_start": float(zero.iterations.mean()),
+                                  "mean_iterations_learned_start": float(warm.iterations.mean())},
+                      "training": {"pairs": len(a_tr), "pair_generation_s": round(gen_s, 2), "steps": steps,
+                                   "seconds": round(train_s, 2), "loss_first": float(losses[0]),
+                                   "loss_last": float(np.mean(losses[-20:]))}}
+    out["chosen_vs_plain"] = round(out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"], 3)
+    return out
 
 
-def run_reference(args, rank: int, world: int) -> dict | None:
-    if rank != 0:
-        return None
-    import oracle
+# ---------------------------------------------------------- profiling driver
 
-    cores = oracle.cpu_count()
-    oracle.set_threads(cores)
-    bigs = [field(N_BIG, q, HI_BIG, LO_BIG) for q in SEEDS_BIG]
-    for _ in range(min(args.warmup, 1)):
-        oracle.solve(bigs[0], tol=TOL)
-    steps = max(1, min(args.steps, 5))
-    times = []
-    for _ in range(steps):  # a step: the 8 fields, one solve each
-        t0 = time.perf_counter()
-        its = [oracle.solve(a, tol=TOL)["iterations"] for a in bigs]
-        times.append((time.perf_counter() - t0) * 1e3 / len(bigs))
-    batch = small_batch(1024)
-    oracle.solve_batch(batch[:64], tol=TOL, threads=cores)
-    t0 = time.perf_counter()
-    oracle.solve_batch(batch, tol=TOL, threads=cores)
-    bsec = time.perf_counter() - t0
-    value = sum(times) / len(times)
-    return {
-        "impl": "reference",
-        "metric": METRIC,
-        "value": round(value, 2),
-        "unit": "ms/solve",
-        "n_gpus": world,
-        "steps": steps,
-        "warmup": args.warmup,
-        "ms_per_step": round(value * len(bigs), 2),
-        "higher_is_better": False,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f64",
-        "data": "synthetic: two-phase GRF fields (reference generator construction), seeded",
-        "config": {"workload": WORKLOAD,
-                   "form": "reference algorithm on the host CPU (oracle C port, OpenMP), one solve per call"},
-        "iterations": its,
-        "batch64": {"metric": "64x64 solves/s (1024 problems, seeds 0..1023, {12,3})",
-                    "value": round(1024 / bsec, 1), "unit": "solves/s"},
-        "cpu_baseline": {"value": round(value, 2), "unit": "ms/solve", "cores": cores, "kind": "port",
-                         "sample": f"{steps} step(s) of the 8-field 1024x1024 workload, mean per solve"},
-        "e2e": {"value": round(value, 2), "unit": "ms/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+def profile(args) -> int:
+    """Runs one workload a few times for a kernel profiler to watch:
+
+    * `solve`: the 1024 x 1024 headline field (seed 1, {1e3, 1e-3}; other
+      sides seed 0 and {12, 3}), with the host-driven CG loop unless
+      --device-loop (a kernel profiler cannot replay the graph's while loop);
+    * `kernels`: each kernel of one CG iteration timed back to back
+      (dgpu_profile_kernels), launched directly on the stream;
+    * `batch`: the batched solve of --count problems of side --n;
+    * `net`: a few training steps of the warm-start network, then one prediction.
+    """
+    if args.profile in ("solve", "kernels") and not args.device_loop:
+        os.environ.setdefault("DARCY_GPU_LOOP", "host")
+    if args.profile == "kernels":
+        os.environ.setdefault("DARCY_GPU_PROFILE_DIRECT", "1")
+    import darcy_cpp_gb300 as darcy
+
+    big = args.n >= 1024
+    hi, lo = (1e3, 1e-3) if big else (12.0, 3.0)
+    if args.profile == "solve":
+        a = field(args.n, 1 if big else 0, hi, lo)
+        for _ in range(args.reps):
+            r = darcy.solve(a, form=args.form)
+        print(f"solve n={args.n} form={args.form}: {r.iterations} iterations, converged {r.converged}")
+    elif args.profile == "kernels":
+        from darcy_cpp_gb300.capi import Context
+
+        a = field(args.n, 1 if big else 0, hi, lo)
+        for row in Context().profile_kernels(a, reps=args.reps, form=args.form):
+            print(f"{row['name']:24s} {row['avg_ms'] * 1e3:9.2f} us  {row['bytes'] / 1e6:9.2f} MB  "
+                  f"x{row['launches_per_iteration']:g} per iteration")
+    elif args.profile == "batch":
+        b = np.stack([field(args.n, s, 12.0, 3.0) for s in range(args.count)])
+        for _ in range(args.reps):
+            t0 = time.perf_counter()
+            r = darcy.solve_batch(b, form=args.form)
+            dt = time.perf_counter() - t0
+        print(f"batch {args.count} x {args.n}^2 form={args.form}: {args.count / dt:.0f} solves/s, "
+              f"mean {r.iterations.mean():.1f} iterations")
+    else:
+        from darcy_cpp_gb300 import learn
+
+        a, u = learn.generate_pairs(range(args.count), args.side)
+        net = learn.WarmStartNet(args.side)
+        losses = net.fit(a, u, steps=args.train_steps, batch=min(256, args.count))
+        u0 = net.predict(a)
+        print(f"net side={args.side}: {args.train_steps} steps, loss {losses[-1]:.4g}, predicted {u0.shape}")
+    return 0
 
 
 def main() -> None:
@@ -497,7 +861,18 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    prof = ap.add_argument_group("profiling driver")
+    prof.add_argument("--profile", choices=["solve", "batch", "net", "kernels"])
+    prof.add_argument("--n", type=int, default=1024)
+    prof.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
+    prof.add_argument("--reps", type=int, default=2)
+    prof.add_argument("--count", type=int, default=304)
+    prof.add_argument("--side", type=int, default=64)
+    prof.add_argument("--train-steps", type=int, default=3)
+    prof.add_argument("--device-loop", action="store_true")
     args = ap.parse_args()
+    if args.profile:
+        sys.exit(profile(args))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":

@@ -1,9 +1,8 @@
 """ctypes binding of the C ABI (include/darcy_gpu.h).
 
-This is the binding a caller without the pybind11 extension would write -- the
-same shape as the `ctypes` stub in INTEGRATION.md -- and the route the
-benchmark and the C-ABI tests use: plain pointers and sizes, host or device
-buffers, status codes, `dgpu_last_error()` for messages.
+This is the binding a caller without the pybind11 extension would write, and
+the route the benchmark and the C-ABI tests use: plain pointers and sizes,
+host or device buffers, status codes, `dgpu_last_error()` for messages.
 """
 
 from __future__ import annotations
@@ -101,6 +100,7 @@ def lib() -> ctypes.CDLL:
         L.dgpu_net_set_scaling.argtypes = [_P, _P]
         L.dgpu_net_set_engine.argtypes = [_P, ctypes.c_int]
         L.dgpu_net_set_loss.argtypes = [_P, ctypes.c_int]
+        L.dgpu_net_set_first_wait.argtypes = [_P, ctypes.c_longlong]
         L.dgpu_net_load_pairs.argtypes = [_P, _P, _P, _P, ctypes.c_int64]
         L.dgpu_net_train.argtypes = [_P, ctypes.c_int64, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong, _P]
         L.dgpu_net_gradients.argtypes = [_P, _P, _P, _P, ctypes.c_int64, _P, _P]
@@ -275,10 +275,10 @@ class Context:
 
     def profile_kernels(self, a, reps: int = 20, **kw) -> list[dict]:
         a = _f64(a)
-        rows = (KernelTime * 32)()
+        rows = (KernelTime * 64)()
         count = ctypes.c_int()
         opt = options(**kw)
-        check(lib().dgpu_profile_kernels(self.handle, _ptr(a), a.shape[0], ctypes.byref(opt), int(reps), rows, 32,
+        check(lib().dgpu_profile_kernels(self.handle, _ptr(a), a.shape[0], ctypes.byref(opt), int(reps), rows, 64,
                                          ctypes.byref(count)))
         return [{"name": r.name.decode(), "avg_ms": r.avg_ms, "bytes": r.bytes,
                  "launches_per_iteration": r.launches_per_iteration} for r in rows[: count.value]]
@@ -366,6 +366,11 @@ class Net:
 
     def set_engine(self, engine: str) -> None:
         check(lib().dgpu_net_set_engine(self.handle, ENGINE[engine]))
+
+    def set_first_wait(self, polls: int) -> None:
+        """Test hook: polls of each tensor-core convolution CTA's first MMA
+        wait (dgpu_net_set_first_wait; default 1 << 24, 0 = run out at once)."""
+        check(lib().dgpu_net_set_first_wait(self.handle, int(polls)))
 
     def set_loss(self, kind: str) -> None:
         check(lib().dgpu_net_set_loss(self.handle, LOSS[kind]))
