@@ -52,7 +52,6 @@ struct BatchArgs {
     int f_shared;               // f is one n*n array shared by every problem
     const double* u0;           // packed warm start, or null
     double* u;                  // packed solution (device)
-    double* u_host;             // if set: the kernel also writes each solution here (host memory it can address)
     int* iterations;
     double* residual;
     int* converged;
@@ -89,16 +88,6 @@ int num_levels_for(int n);
 
 // Message returned by dgpu_last_error() on this thread (solver.cu).
 void set_last_error(const char* msg);
-
-// Coarse levels of the W-cycle in one thread-block cluster (cluster.cuh).
-template <class T>
-struct ClusterArgs;
-template <class T>
-size_t cluster_cycle_smem(const ClusterArgs<T>& A);
-template <class T>
-bool cluster_cycle_supported(const ClusterArgs<T>& A, int ctas);
-template <class T>
-void launch_cluster_cycle(const ClusterArgs<T>& A, int ctas, cudaStream_t s);
 
 // Learned warm start (learn.cu), for the batched solve.
 int net_predict_on_stream(dgpu_net* net, const double* d_a, double fscalar, int64_t count, double* d_u0,

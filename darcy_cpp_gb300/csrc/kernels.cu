@@ -15,7 +15,6 @@
 #include <map>
 
 #include "block.cuh"
-#include "cluster.cuh"
 #include "cycle.cuh"
 #include "engine.h"
 #include "fused.cuh"
@@ -975,7 +974,6 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
     if (bnorm == 0.0) {
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
             u[k] = 0.0;
-            if (A.u_host) A.u_host[off + k] = 0.0;
         }
         if (threadIdx.x == 0) {
             A.bad[pid] = ~0ull;
@@ -1062,8 +1060,6 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         }
         true_res = sqrt(block_sum_wide(tr, red)) / bnorm;
     }
-    if (A.u_host)
-        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) A.u_host[off + k] = u[k];
     if (threadIdx.x == 0) {
         A.bad[pid] = ~0ull;
         A.iterations[pid] = iterations;
@@ -1118,72 +1114,6 @@ void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream
     cudaFuncSetAttribute(k_block_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     k_block_solve<T><<<ctas, threads, bytes, s>>>(args);
 }
-
-// ------------------------------------------------------ coarse-level cluster
-
-template <class T>
-size_t cluster_cycle_smem(const ClusterArgs<T>& A) {
-    return sizeof(T) * (size_t)cluster_layout<T>(A).total;
-}
-
-// Whether a cluster of `ctas` CTAs with this shared memory can be resident.
-template <class T>
-bool cluster_cycle_supported(const ClusterArgs<T>& A, int ctas) {
-    const size_t smem = cluster_cycle_smem<T>(A);
-    if (smem > 227 * 1024) return false;
-    if (cudaFuncSetAttribute(k_cluster_cycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(ctas);
-    cfg.blockDim = dim3(kClusterThreads);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = ctas;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int clusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&clusters, k_cluster_cycle<T>, &cfg) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    return clusters > 0;
-}
-
-template <class T>
-void launch_cluster_cycle(const ClusterArgs<T>& A, int ctas, cudaStream_t s) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(ctas);
-    cfg.blockDim = dim3(kClusterThreads);
-    cfg.dynamicSmemBytes = cluster_cycle_smem<T>(A);
-    cfg.stream = s;
-    cudaLaunchAttribute attr[2];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = ctas;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    int na = 1;
-    if (g_pdl) {
-        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[1].val.programmaticStreamSerializationAllowed = 1;
-        na = 2;
-    }
-    cfg.attrs = attr;
-    cfg.numAttrs = na;
-    cudaLaunchKernelEx(&cfg, k_cluster_cycle<T>, A);
-}
-
-template size_t cluster_cycle_smem<float>(const ClusterArgs<float>&);
-template size_t cluster_cycle_smem<double>(const ClusterArgs<double>&);
-template bool cluster_cycle_supported<float>(const ClusterArgs<float>&, int);
-template bool cluster_cycle_supported<double>(const ClusterArgs<double>&, int);
-template void launch_cluster_cycle<float>(const ClusterArgs<float>&, int, cudaStream_t);
-template void launch_cluster_cycle<double>(const ClusterArgs<double>&, int, cudaStream_t);
 
 // ------------------------------------------------------ explicit instantiation
 

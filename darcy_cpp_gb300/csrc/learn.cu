@@ -20,10 +20,14 @@
 // the accumulator back for the epilogue (bias + GELU, or the GELU derivative
 // in the backward pass). The input gradient of a 32 -> 32 layer is the same
 // kernel with the taps flipped and the channel roles of the weights swapped.
-// The 2 -> 32 and 32 -> 1 layers, the weight gradients (reductions over all
-// pixels, written per CTA and summed in a fixed order so training is
-// deterministic) and a CUDA-core version of the 32 -> 32 convolution (used
-// to check the tensor-core one) run on the CUDA cores.
+// The 2 -> 32 layer runs the same kernel on an 8-channel padded input, the
+// 32 -> 1 layer with 16 padded output rows. The weight gradients of every
+// layer are tensor-core GEMMs too (k_wgrad_tc: M = (tap, input channel) rows
+// of an im2col staged in shared memory, N = output channels, K = pixels),
+// written per CTA and summed in a fixed order so training is deterministic.
+// CUDA-core versions of the convolution and of the weight gradients (engine
+// "simt") check the tensor-core ones; the 1 -> 32 input gradient of the
+// output layer stays on the CUDA cores.
 //
 // The reference has no learned component: this file extends its solve path
 // with the warm start x0 that PCG then refines to the same tolerance.
@@ -474,7 +478,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_tc(const bf16* __restrict
                                                           const float* __restrict__ bias, Geom g, int64_t ntiles,
                                                           int mode, const float* __restrict__ aux,
                                                           float* __restrict__ pre, bf16* __restrict__ act,
-                                                          float* __restrict__ outf, int* __restrict__ err) {
+                                                          float* __restrict__ outf, int* __restrict__ err,
+                                                          long long first_wait) {
     using S = TcShape<CCH, NOUT>;
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t stage = tc_stage_bytes(CCH, g.nq);
@@ -507,6 +512,10 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_tc(const bf16* __restrict
     constexpr uint32_t idesc = mma_idesc(kTile, NOUT);
     uint32_t phase = 0;
     int buf = 0;
+    // polls of this CTA's first completion wait (kWaitLimit unless a test
+    // shortens it to make the wait run out); every later wait, and the drain
+    // wait after one ran out, keeps kWaitLimit
+    long long wait_polls = first_wait;
 
     int64_t tile = blockIdx.x;
     if (tile < ntiles) {
@@ -553,7 +562,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_tc(const bf16* __restrict
             stage_tile<CCH>(x, g, pb, s1, x_addr + (buf ^ 1) * stage, plane);
         }
         __syncwarp();
-        const bool ok = __syncthreads_and(mbar_wait(smem_u32(mbar), phase, kWaitLimit));
+        const bool ok = __syncthreads_and(mbar_wait(smem_u32(mbar), phase, wait_polls));
+        wait_polls = kWaitLimit;
         phase ^= 1u;
         if (!ok) {
             if (tid == 0) atomicExch(err, 1);
@@ -722,6 +732,205 @@ __global__ void k_reduce_wgrad(const float* __restrict__ part, int nparts, int n
     }
 }
 
+// Weight gradients on the tensor cores. The same sums as k_wgrad,
+// gW[co][tap * CIN + ci] = sum_p dy[p, co] x[p + shift(tap), ci] and
+// gb[co] = sum_p dy[p, co], as D = A B with M = (tap, input-channel chunk, ci)
+// rows, N = co columns and K = pixels: per tile of 128 positions the CTA
+// stages A as one 128-position plane per (tap, chunk of 8 input channels) --
+// each plane the staged input shifted by the tap (an im2col in shared memory,
+// 16-byte cp.async chunks) -- plus one plane of ones whose D row is the bias
+// gradient, zero planes up to a multiple of 16, and B as one plane per chunk
+// of 8 output channels. Both operands are MN-major core matrices (8 positions
+// x 16 bytes of channels, 128 contiguous bytes): A's 16-plane groups are the
+// M = 128 tiles, K advances 16 positions per MMA. One thread issues MT x 8
+// tcgen05.mma (M 128, N NOUT, K 16, BF16 in, FP32 accumulate) per tile into
+// MT tensor-memory accumulators that persist over all the CTA's tiles (the
+// next tile is staged while they run); at the end each warp reads its 32
+// rows with tcgen05.ld and writes the CTA's partial in the layout
+// k_reduce_wgrad sums in CTA order, so training stays deterministic.
+// An FP32 dy (the output layer's, one channel) enters as a BF16 hi/lo pair in
+// columns 0 and 1, summed in the epilogue.
+template <int CCH, int NOUT>
+struct WgradTc {
+    static constexpr int kDataPlanes = kTaps * CCH;                     // A planes holding x
+    static constexpr int MT = (kDataPlanes + 1 + 15) / 16;              // M = 128 tiles (with the ones plane)
+    static constexpr int kAPlanes = MT * 16;
+    static constexpr int kBPlanes = NOUT / 8;
+    static constexpr int kPlane = kTile * 16;                           // bytes: 128 positions x 16 B
+    static constexpr int kStage = (kAPlanes + kBPlanes) * kPlane;
+    static constexpr int kCols = MT * NOUT <= 32 ? 32 : MT * NOUT <= 64 ? 64 : MT * NOUT <= 128 ? 128 : 256;
+    static constexpr int kSmem = 2 * kStage + 16;
+};
+
+// Instruction descriptor of kind::f16 with both operands MN-major.
+__host__ __device__ constexpr uint32_t mma_idesc_mn(int M, int N) {
+    return mma_idesc(M, N) | (1u << 15) | (1u << 16);
+}
+
+template <int CCH, int NOUT, int CIN, int COUT, class TDY>
+__device__ __forceinline__ void wgrad_stage(const bf16* __restrict__ x, const TDY* __restrict__ dy, const Geom& g,
+                                            int64_t pbase, int s0, unsigned char* buf) {
+    using W = WgradTc<CCH, NOUT>;
+    const int q = threadIdx.x;  // one position of the tile per thread (kConvThreads == kTile)
+    const uint32_t a = smem_u32(buf);
+#pragma unroll 1
+    for (int pl = 0; pl < W::kDataPlanes; ++pl) {
+        const int tap = pl / CCH, c = pl - tap * CCH;
+        const int pix = position_pixel(g, s0 - g.P - 1 + q + (tap / 3) * g.P + tap % 3);
+        const bf16* src = pix >= 0 ? x + ((pbase + pix) * CCH + c) * 8 : x;
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(a + pl * W::kPlane + q * 16), "l"(src),
+                     "r"(pix >= 0 ? 16 : 0)
+                     : "memory");
+    }
+    const int pix = position_pixel(g, s0 + q);
+    const uint32_t b = a + W::kAPlanes * W::kPlane;
+    if constexpr (sizeof(TDY) == 2) {
+#pragma unroll
+        for (int c = 0; c < W::kBPlanes; ++c) {
+            const TDY* src = pix >= 0 ? dy + (pbase + pix) * COUT + c * 8 : dy;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(b + c * W::kPlane + q * 16),
+                         "l"(src), "r"(pix >= 0 ? 16 : 0)
+                         : "memory");
+        }
+    } else {  // one FP32 channel -> BF16 hi in column 0, lo in column 1
+        const float d = pix >= 0 ? to_f(dy[pbase + pix]) : 0.f;
+        const bf16 hi = __float2bfloat16(d);
+        const bf16 lo = __float2bfloat16(d - __bfloat162float(hi));
+        __nv_bfloat162 pr;
+        pr.x = hi;
+        pr.y = lo;
+        uint4 row = make_uint4(*reinterpret_cast<const uint32_t*>(&pr), 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(buf + W::kAPlanes * W::kPlane + q * 16) = row;
+#pragma unroll
+        for (int c = 1; c < W::kBPlanes; ++c)
+            *reinterpret_cast<uint4*>(buf + (W::kAPlanes + c) * W::kPlane + q * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int CCH, int NOUT, int CIN, int COUT, class TDY>
+__global__ void __launch_bounds__(kConvThreads) k_wgrad_tc(const bf16* __restrict__ x, const TDY* __restrict__ dy,
+                                                           Geom g, int64_t ntiles, float* __restrict__ part,
+                                                           int* __restrict__ err, long long first_wait) {
+    using W = WgradTc<CCH, NOUT>;
+    static_assert(kConvThreads == kTile, "one staged position per thread");
+    constexpr int K = kTaps * CIN;
+    constexpr int NV = (K + 1) * COUT;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + 2 * W::kStage);
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // constant planes of both stages: the ones plane (bias row) and zeros up
+    // to the M tile boundary; staging never writes them
+    for (int st = 0; st < 2; ++st)
+        for (int pl = W::kDataPlanes; pl < W::kAPlanes; ++pl) {
+            const uint32_t one = pl == W::kDataPlanes ? 0x3F803F80u : 0u;  // BF16 1.0 pairs
+            *reinterpret_cast<uint4*>(sm + st * W::kStage + pl * W::kPlane + tid * 16) = make_uint4(one, one, one, one);
+        }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"((uint32_t)W::kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init(smem_u32(mbar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    constexpr uint32_t idesc = mma_idesc_mn(kTile, NOUT);
+    uint32_t phase = 0;
+    int buf = 0;
+    bool any = false, failed = false;
+    long long wait_polls = first_wait;
+
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles) {
+        int64_t pb;
+        int s0;
+        tile_origin(tile, g, pb, s0);
+        wgrad_stage<CCH, NOUT, CIN, COUT, TDY>(x, dy, g, pb, s0, sm);
+    }
+    for (; tile < ntiles; tile += gridDim.x) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t base = smem_u32(sm + buf * W::kStage);
+            const uint32_t bb = base + W::kAPlanes * W::kPlane;
+#pragma unroll 1
+            for (int ks = 0; ks < kTile / 16; ++ks)
+#pragma unroll
+                for (int mt = 0; mt < W::MT; ++mt) {
+                    // MN-major, no swizzle: element (mn, k) at start + (mn / 8) * SBO + (mn % 8) * 2
+                    // + (k / 8) * LBO + (k % 8) * 16, with SBO = one plane and LBO = 8 positions
+                    const uint64_t ad = smem_desc(base + mt * 16 * W::kPlane + ks * 256, 128, W::kPlane);
+                    const uint64_t bd = smem_desc(bb + ks * 256, 128, W::kPlane);
+                    mma_bf16(tmem + mt * NOUT, ad, bd, idesc, (any || ks > 0) ? 1u : 0u);
+                }
+            mma_commit(smem_u32(mbar));
+        }
+        any = true;
+        const int64_t next = tile + gridDim.x;
+        if (next < ntiles) {  // stage the next tile while these MMAs run
+            int64_t pb;
+            int s1;
+            tile_origin(next, g, pb, s1);
+            wgrad_stage<CCH, NOUT, CIN, COUT, TDY>(x, dy, g, pb, s1, sm + (buf ^ 1) * W::kStage);
+        }
+        __syncwarp();
+        const bool ok = __syncthreads_and(mbar_wait(smem_u32(mbar), phase, wait_polls));
+        wait_polls = kWaitLimit;
+        phase ^= 1u;
+        if (!ok) {
+            if (tid == 0) atomicExch(err, 1);
+            // the MMAs in flight get a bounded chance to land before the
+            // tensor memory is released
+            mbar_wait(smem_u32(mbar), phase ^ 1u, kWaitLimit);
+            failed = true;
+            break;
+        }
+        buf ^= 1;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (any && !failed) {
+        float* out = part + (int64_t)blockIdx.x * NV;
+        const int r = warp * 32 + lane;  // row of D (tensor-memory lane)
+#pragma unroll 1
+        for (int mt = 0; mt < W::MT; ++mt) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + mt * NOUT, v);
+            const int pl = mt * 16 + r / 8, e = r % 8;
+            int k = -1;
+            if (pl < W::kDataPlanes) {
+                const int tap = pl / CCH, ci = (pl - tap * CCH) * 8 + e;
+                if (ci < CIN) k = tap * CIN + ci;
+            } else if (pl == W::kDataPlanes && e == 0) {
+                k = K;  // the ones plane: bias gradient
+            }
+            if (k >= 0) {
+                if constexpr (sizeof(TDY) == 2) {
+#pragma unroll
+                    for (int co = 0; co < COUT; ++co) out[co * (K + 1) + k] = v[co];
+                } else {
+                    out[k] = v[0] + v[1];
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)W::kCols)
+                     : "memory");
+}
+
 // ---------------------------------------------------------------- loss
 
 constexpr int kLossBlocks = 256, kLossThreads = 256;
@@ -863,6 +1072,7 @@ struct dgpu_net {
     Geom g{};
     int hw = 0;
     int engine = DGPU_NET_TENSOR;
+    long long first_wait = kWaitLimit;  // polls of each conv CTA's first MMA wait (test hook)
     LayerTable T{};
     int nparams = 0;
     int64_t nwb = 0;
@@ -957,7 +1167,7 @@ void launch_tc(dgpu_net* N, int ctas_cap, const bf16* x, const bf16* wB, const f
     const int64_t ntiles = count * N->g.tiles_per_img;
     const int ctas = (int)std::min<int64_t>(ntiles, ctas_cap);
     k_conv_tc<CCH, NOUT><<<ctas, kConvThreads, tc_smem_bytes<CCH, NOUT>(N->g.nq), N->stream>>>(
-        x, wB, b, N->g, ntiles, mode, aux, pre, act, outf, N->err.p);
+        x, wB, b, N->g, ntiles, mode, aux, pre, act, outf, N->err.p, N->first_wait);
     launched(N);
 }
 
@@ -1005,9 +1215,22 @@ template <class TDY, int CIN, int XS, int COUT>
 void wgrad(dgpu_net* N, const bf16* x, const TDY* dy, int64_t count, int layer) {
     using WG = Wgrad<CIN, COUT>;
     const int64_t ntiles = count * N->g.tiles_per_img;
-    const int ctas = (int)std::min<int64_t>(ntiles, N->wg_ctas);
-    k_wgrad<TDY, CIN, XS, COUT><<<ctas, WG::kThreads, wgrad_smem(N->g, CIN, COUT), N->stream>>>(x, dy, N->g, ntiles,
-                                                                                              N->gpart.p);
+    int ctas;
+    if (N->engine == DGPU_NET_TENSOR) {
+        // tensor cores: one CTA per SM (two ~100 KB stages of shared memory)
+        constexpr int CCH = XS / 8;
+        constexpr int NOUT = COUT == 1 ? 16 : COUT;
+        using W = WgradTc<CCH, NOUT>;
+        NCK(cudaFuncSetAttribute(k_wgrad_tc<CCH, NOUT, CIN, COUT, TDY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 W::kSmem));
+        ctas = (int)std::min<int64_t>(ntiles, N->sms);
+        k_wgrad_tc<CCH, NOUT, CIN, COUT, TDY><<<ctas, kConvThreads, W::kSmem, N->stream>>>(
+            x, dy, N->g, ntiles, N->gpart.p, N->err.p, N->first_wait);
+    } else {
+        ctas = (int)std::min<int64_t>(ntiles, N->wg_ctas);
+        k_wgrad<TDY, CIN, XS, COUT><<<ctas, WG::kThreads, wgrad_smem(N->g, CIN, COUT), N->stream>>>(x, dy, N->g,
+                                                                                                  ntiles, N->gpart.p);
+    }
     launched(N);
     k_reduce_wgrad<<<grid_for(WG::NV, 256, N->sms), 256, 0, N->stream>>>(
         N->gpart.p, ctas, WG::NV, WG::K, N->grad.p + N->T.off_w[layer], N->grad.p + N->T.off_b[layer]);
@@ -1426,6 +1649,15 @@ int dgpu_net_set_engine(dgpu_net* net, int engine) {
         if (engine != DGPU_NET_TENSOR && engine != DGPU_NET_SIMT) net_invalid("unknown engine");
         std::lock_guard<std::mutex> lock(net->mu);
         net->engine = engine;
+    });
+}
+
+int dgpu_net_set_first_wait(dgpu_net* net, long long polls) {
+    return net_run([&] {
+        check_net(net);
+        if (polls < 0) net_invalid("polls must be >= 0");
+        std::lock_guard<std::mutex> lock(net->mu);
+        net->first_wait = polls > kWaitLimit ? kWaitLimit : polls;
     });
 }
 

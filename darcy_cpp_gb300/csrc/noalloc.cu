@@ -20,7 +20,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "../../include/darcy_gpu.h"
@@ -36,12 +35,8 @@ constexpr size_t kStatusOffset = kNoAllocBytes - 256;  // last 256 bytes: status
 
 // Scratch of the allocation-free entry point (see the file comment). In host
 // code this name is only a stand-in for the device symbol: its device address
-// comes from cudaGetSymbolAddress, fetched once per device.
+// comes from cudaGetSymbolAddress on the current device, on every call.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
 
 // One cycle z = M r for a side-n problem, one CTA, all scratch in `scratch`.
 __global__ void __launch_bounds__(256) k_precondition_noalloc(unsigned char* scratch, int n, int pre, int post,
@@ -69,22 +64,16 @@ __global__ void __launch_bounds__(256) k_precondition_noalloc(unsigned char* scr
     for (int64_t k = threadIdx.x; k < m; k += blockDim.x) z[k] = V.cg[4][k];
 }
 
-// Device address of the scratch array on the current device, looked up the
-// first time this device is used (so that first call must not be made while
-// a stream capture is in progress on the device).
+// Device address of the scratch array in the current device's context. It is
+// looked up on every call (a table lookup once the module is loaded; the first
+// call on a device loads it): a cached address would go stale when the
+// context is reset (cudaDeviceReset reloads the module, and the array can
+// move).
 int scratch_address(void** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return (int)e;
-    if (dev < 0 || dev >= kMaxDevices) return (int)cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess) return (int)e;
-        g_scratch_addr[dev] = ptr;
-    }
-    *out = g_scratch_addr[dev];
+    *out = ptr;
     return 0;
 }
 
@@ -108,11 +97,15 @@ extern "C" int dgpu_apply_preconditioner_noalloc(const double* d_a, const double
         set_last_error("buffers must not be NULL");
         return DGPU_INVALID_INPUT;
     }
-    if (pre_sweeps < 1 || post_sweeps < 1) {  // bindings.cpp:235
+    // The reference's sweep and cycle checks (src/bindings.cpp:231-232). The
+    // reference validates the permeability first (src/bindings.cpp:225); here
+    // that check runs in the kernel, after these, so an input invalid both
+    // ways reports the sweep/cycle error.
+    if (pre_sweeps < 1 || post_sweeps < 1) {
         set_last_error("sweeps must be at least 1");
         return DGPU_INVALID_INPUT;
     }
-    if (cycle_index < 1 || cycle_index > 2) {  // bindings.cpp:236
+    if (cycle_index < 1 || cycle_index > 2) {
         set_last_error("cycle_index must be 1 or 2");
         return DGPU_INVALID_INPUT;
     }

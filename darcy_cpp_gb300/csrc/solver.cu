@@ -29,7 +29,6 @@
 
 #include "../../include/darcy_gpu.h"
 #include "engine.h"
-#include "cluster.cuh"
 
 using namespace dgpu;
 
@@ -188,7 +187,6 @@ struct GridPlan {
     int ntail = 0;                  // cells of the first tail level (dense operator is ntail x ntail)
     int64_t m = 0;
     bool mixed_mg = false;
-    int cl0 = -1, cl_nl = 0, cl_ctas = 0;  // coarse levels run by one thread-block cluster (cl0 = top), or -1
     int lf = 0;  // first level of the fused visits (the levels above it run the unfused kernels)
     Arena arena;
     double *a = nullptr, *f = nullptr, *u0 = nullptr, *u = nullptr;
@@ -238,7 +236,6 @@ struct dgpu_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
     bool cond_ok = false;
-    bool host_direct = false;  // kernels may read/write pageable host arrays (ATS over NVLink-C2C)
     cudaStream_t copy_stream = nullptr;  // host<->device copies of pipelined batches
     cudaStream_t stream2 = nullptr;      // second compute stream of pipelined batches
     std::vector<cudaEvent_t> chunk_events;
@@ -293,45 +290,6 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
             P.tail_l0 = l;
             break;
         }
-    // Coarse levels in one cluster (fused visits only, opt-in with
-    // DARCY_GPU_CLUSTER=1): the first level below the finest with side <= 128
-    // is the cluster's top, the first level with side <= 16 its dense tail.
-    // Measured on GB300 at 1024^2: 83.8 / 74.4 ms (FP64 / mixed) against 46.1 /
-    // 38.4 ms with one launch per visit -- each of the ~78 cluster-barrier
-    // phases of a launch costs ~1.9 us, more than the launches it replaces.
-    P.cl0 = -1;
-    {
-        const char* ce = std::getenv("DARCY_GPU_CLUSTER");
-        const bool want = K.pre == 1 && K.post == 1 && K.pc == kPcMultigrid && ce && std::strcmp(ce, "1") == 0;
-        int top = -1, tl = -1;
-        for (int l = 1; l < P.nlev && top < 0; ++l)
-            if (sides[l] <= kClusterTopRows * kClusterMaxCtas) top = l;
-        for (int l = 0; l < P.nlev && tl < 0; ++l)
-            if (sides[l] <= 16) tl = l;
-        if (want && top >= 1 && tl > top && tl - top <= kClusterMaxLevels) {
-            const int ctas = (sides[top] + kClusterTopRows - 1) / kClusterTopRows;
-            bool ok;
-            if (P.mixed_mg) {
-                ClusterArgs<float> probe{};
-                probe.nl = tl - top;
-                for (int i = 0; i < probe.nl; ++i) probe.lv[i].n = sides[top + i];
-                probe.n_tail = sides[tl];
-                ok = cluster_cycle_supported<float>(probe, ctas);
-            } else {
-                ClusterArgs<double> probe{};
-                probe.nl = tl - top;
-                for (int i = 0; i < probe.nl; ++i) probe.lv[i].n = sides[top + i];
-                probe.n_tail = sides[tl];
-                ok = cluster_cycle_supported<double>(probe, ctas);
-            }
-            if (ok) {
-                P.cl0 = top;
-                P.cl_nl = tl - top;
-                P.cl_ctas = ctas;
-                P.tail_l0 = tl;
-            }
-        }
-    }
     P.ntail = sides[P.tail_l0] * sides[P.tail_l0];
     const size_t m = (size_t)P.m;
     P.h.assign(P.nlev, Lvl64{});
@@ -347,7 +305,6 @@ void alloc_plan(dgpu_context* C, GridPlan& P) {
     if (P.fused) {
         const int side = unfused_side();
         while (P.lf < P.tail_l0 && sides[P.lf] >= side) ++P.lf;
-        if (P.cl0 >= 0 && P.lf > P.cl0 - 1) P.lf = std::max(0, P.cl0 - 1);  // keep the cluster's parent fused
     }
     auto layout = [&](Carver& A) {
         P.a = A.take<double>(m);
@@ -503,7 +460,7 @@ VisitLevel<float> visit_level<float>(const GridPlan& P, int l) {
 // every post-visit that is directly followed by the next call's pre-visit of
 // the same level into one kernel, then launches the list; iterates alternate
 // between the level's two buffers, `cur` tracking which holds each level's.
-enum VisitKind { kOpPre, kOpPost, kOpMid, kOpTail, kOpCluster };
+enum VisitKind { kOpPre, kOpPost, kOpMid, kOpTail };
 struct VisitOp {
     int kind, l;
     bool first;
@@ -513,8 +470,6 @@ void collect_visits(const GridPlan& P, int l, bool first, std::vector<VisitOp>& 
     ops.push_back({kOpPre, l, first});
     if (l + 1 >= P.tail_l0)
         ops.push_back({kOpTail, l, false});
-    else if (l + 1 == P.cl0)
-        ops.push_back({kOpCluster, l, false});
     else
         for (int g = 0; g < P.key.gamma; ++g) collect_visits(P, l + 1, g == 0, ops);
     ops.push_back({kOpPost, l, false});
@@ -560,20 +515,6 @@ void emit_visit_fused(GridPlan& P, std::vector<int>& cur, cudaStream_t s, int l_
                 launch_tail_matvec<T>(tail_matrix<T>(P), P.ntail, lv[l + 1].b, X(l + 1, 0), P.st, s);
                 cur[l + 1] = 0;
                 break;
-            case kOpCluster: {  // the whole coarse-grid correction in one cluster launch
-                ClusterArgs<T> CA{};
-                CA.nl = P.cl_nl;
-                for (int i = 0; i < P.cl_nl; ++i) CA.lv[i] = visit_level<T>(P, P.cl0 + i);
-                CA.n_tail = P.h[P.tail_l0].n;
-                CA.tail = tail_matrix<T>(P);
-                CA.b_top = lv[l + 1].b;
-                CA.x_top = X(l + 1, 0);
-                CA.gamma = K.gamma;
-                CA.top_calls = K.gamma;
-                launch_cluster_cycle<T>(CA, P.cl_ctas, s);
-                cur[l + 1] = 0;
-                break;
-            }
             case kOpPost:
                 launch_visit_post<T>(V, X(l, cur[l]), X(l + 1, cur[l + 1]), X(l, cur[l] ^ 1),
                                      l == 0 ? P.r : nullptr, P.st, P.partials, s);
@@ -1156,17 +1097,15 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sides[x] > sides[y]; });
 
     // host arrays read and written by the kernel itself (no staging copies)
-    const bool direct = C->host_direct && !device_ptrs;
     BatchArgs A{};
     A.count = (int)count;
-    A.a = direct ? a : C->ba.ensure(total);
+    A.a = C->ba.ensure(total);
     A.u = C->bu.ensure(total);
-    A.u_host = direct ? u_out : nullptr;
     A.f = nullptr;
-    if (f) A.f = direct ? f : C->bf.ensure(f_shared ? (size_t)sides[0] * sides[0] : (size_t)total);
+    if (f) A.f = C->bf.ensure(f_shared ? (size_t)sides[0] * sides[0] : (size_t)total);
     A.f_shared = f_shared;
     A.fscalar = fscalar;
-    A.u0 = u0 ? (direct ? u0 : C->bu0.ensure(total)) : nullptr;
+    A.u0 = u0 ? C->bu0.ensure(total) : nullptr;
     A.order = C->border.ensure(count);
     A.side = C->bside.ensure(count);
     A.off = C->boff.ensure(count);
@@ -1194,7 +1133,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
     // compute hides.
     const auto tuned_hit = C->tuned.find(tune_key(C, maxside, mixed, o, count));
     const int64_t resident = 2 * (int64_t)C->sms;
-    const bool pipelined = !direct && !device_ptrs && !warm && tuned_hit != C->tuned.end() &&
+    const bool pipelined = !device_ptrs && !warm && tuned_hit != C->tuned.end() &&
                            count >= 4 * resident && !(o->record_history);
     std::vector<int64_t> cut{0, count};
     if (pipelined) {
@@ -1216,7 +1155,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         const int64_t hi = off[p1 - 1] + (int64_t)sides[p1 - 1] * sides[p1 - 1];
         return {lo, hi - lo};
     };
-    if (!direct && !pipelined) {
+    if (!pipelined) {
         CK(cudaMemcpyAsync((void*)A.a, a, sizeof(double) * total, in, s));
         if (f)
             CK(cudaMemcpyAsync((void*)A.f, f,
@@ -1364,8 +1303,8 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         CK(cudaStreamWaitEvent(s, C->chunk_events[2 * nch - 1], 0));
     } else {
         launch(cfg, count);
-        if (!direct && !device_ptrs) prefault_output(u_out, total);
-        if (!direct) CK(cudaMemcpyAsync(u_out, A.u, sizeof(double) * total, outk, s));
+        if (!device_ptrs) prefault_output(u_out, total);
+        CK(cudaMemcpyAsync(u_out, A.u, sizeof(double) * total, outk, s));
     }
     std::vector<unsigned long long> bad(count);
     CK(cudaMemcpyAsync(bad.data(), A.bad, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
@@ -1544,26 +1483,14 @@ int dgpu_create(int device, dgpu_context** out) {
         C->cond_ok = !(loop && std::strcmp(loop, "host") == 0) && conditional_nodes_work(C->stream);
         const char* pdl = std::getenv("DARCY_GPU_PDL");
         set_programmatic_launch(!(pdl && std::strcmp(pdl, "0") == 0));
-        // Host arrays addressed directly by the batched kernel (opt-in,
-        // DARCY_GPU_HOST_DIRECT=1), only where the device reads pageable
-        // memory through the host's own page tables. Measured on GB300 + Grace:
-        // 3x slower than the pipelined copies for 4096 x 64^2 (34.5 against
-        // 11.1 ms with one CG iteration), so the copies are the default.
-        int pageable = 0, host_tables = 0;
-        CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device));
-        CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device));
-        const char* direct = std::getenv("DARCY_GPU_HOST_DIRECT");
-        C->host_direct = pageable == 1 && host_tables == 1 && direct && std::strcmp(direct, "1") == 0;
         CK(cudaStreamCreateWithFlags(&C->copy_stream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&C->stream2, cudaStreamNonBlocking));
         char buf[512];
         std::snprintf(buf, sizeof buf,
-                      "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s | programmatic launch: %s"
-                      " | batch host arrays: %s",
+                      "%s | %d SMs | sm_%d%d | %.1f GiB | L2 %.1f MiB | graph while-loop: %s | programmatic launch: %s",
                       prop.name, prop.multiProcessorCount, prop.major, prop.minor,
                       prop.totalGlobalMem / 1073741824.0, prop.l2CacheSize / 1048576.0,
-                      C->cond_ok ? "device-side" : "host-chunked", programmatic_launch() ? "on" : "off",
-                      C->host_direct ? "addressed directly" : "copied");
+                      C->cond_ok ? "device-side" : "host-chunked", programmatic_launch() ? "on" : "off");
         C->info = buf;
         *out = C.release();
     });
@@ -1928,7 +1855,7 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
         int visits_tail = 1;  // tail products per iteration: parent visits = gamma^(tail_l0 - 1)
         for (int l = 1; l < P.tail_l0; ++l) visits_tail *= K.gamma;
         struct Item {
-            const char* name;
+            std::string name;
             double bytes, per_it;
             std::function<void()> launch;
         };
@@ -1983,10 +1910,57 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
             items.push_back({"tail_matvec", w * (nt * nt + 2 * nt), (double)visits_tail,
                              [=] { launch_tail_matvec<T>(Tm, ntail, L1.b, L1.x, stp, s); }});
         };
-        if (f32)
+        // The fused visits of the coarse levels (side < the unfused-kernel
+        // side, above the dense tail), by kind and level, with their launches
+        // per preconditioner application: the fused program from level lf runs
+        // once per visit of level lf - 1, i.e. gamma^(lf - 1) times per cycle.
+        auto add_coarse = [&](auto tag) {
+            using T = decltype(tag);
+            if (!P.fused || P.tail_l0 <= 1) return;
+            const auto& lv = levels_of<T>(P);
+            const int lf = P.lf;
+            int reps_top = 1;
+            for (int l = 1; l < lf; ++l) reps_top *= K.gamma;
+            const std::vector<VisitOp> prog = lf == 0 ? visit_program(P, 0, 1) : visit_program(P, lf, K.gamma);
+            // (kind, level, first) -> launches per cycle
+            std::map<std::tuple<int, int, bool>, int> counts;
+            for (const VisitOp& op : prog)
+                if (op.kind != kOpTail && op.l >= 1) counts[{op.kind, op.l, op.kind == kOpPre && op.first}] += reps_top;
+            const double cb = sizeof(T) == 4 ? 7 * 4.0 : 4 * 8.0;  // staged coefficient bytes per cell
+            for (const auto& kv : counts) {
+                const int kind = std::get<0>(kv.first), l = std::get<1>(kv.first);
+                const bool first = std::get<2>(kv.first);
+                const VisitLevel<T> V = visit_level<T>(P, l);
+                T* x0 = (T*)P.X0[l];
+                T* x1 = (T*)P.X1[l];
+                T* xc = (T*)P.X0[l + 1];
+                T* bc = lv[l + 1].b;
+                const double ml = (double)V.n * V.n;
+                const int ncl = (V.n + 1) / 2;
+                const double mcl = (double)ncl * ncl;
+                char nm[48];
+                if (kind == kOpPre) {
+                    std::snprintf(nm, sizeof nm, "visit_pre%s(l%d)", first ? "_zero" : "", l);
+                    items.push_back({nm, cb * ml + w * ((first ? 2 : 3) * ml + mcl),
+                                     (double)kv.second, [=] { launch_visit_pre<T>(V, first ? nullptr : x0, x1, bc, s); }});
+                } else if (kind == kOpMid) {
+                    std::snprintf(nm, sizeof nm, "visit_mid(l%d)", l);
+                    items.push_back({nm, cb * ml + w * (3 * ml + 2 * mcl), (double)kv.second,
+                                     [=] { launch_visit_mid<T>(V, x0, xc, x1, bc, s); }});
+                } else {
+                    std::snprintf(nm, sizeof nm, "visit_post(l%d)", l);
+                    items.push_back({nm, 3 * w * ml + w * (3 * ml + mcl), (double)kv.second,
+                                     [=] { launch_visit_post<T>(V, x0, xc, x1, nullptr, stp, partials, s); }});
+                }
+            }
+        };
+        if (f32) {
             add_level0(float{});
-        else
+            add_coarse(float{});
+        } else {
             add_level0(double{});
+            add_coarse(double{});
+        }
         const Lvl64 H0 = P.h[0];
         double* const pv = P.p;
         double* const apv = P.ap;
@@ -2037,7 +2011,7 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
             if (x) cudaGraphExecDestroy(x);
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-            std::snprintf(out[q].name, sizeof out[q].name, "%s", it.name);
+            std::snprintf(out[q].name, sizeof out[q].name, "%s", it.name.c_str());
             out[q].avg_ms = ms / reps;
             out[q].bytes = it.bytes;
             out[q].launches_per_iteration = it.per_it;

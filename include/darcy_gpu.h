@@ -168,11 +168,13 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
  * buffers a, r, z (n*n doubles each) and an optional cudaStream_t; the
  * scratch is a fixed 2 MiB array inside the library, present on every device
  * that loads it until the process exits, so n is limited to 1..128 (larger n
- * returns DGPU_INVALID_INPUT). No context is needed and nothing is allocated:
- * the first call on a device looks up the array's device address (make that
- * first call outside any stream capture). All calls share the one array, so
- * calls that overlap on the GPU race; serialise them. Blocks until z is
- * written (it reads back a status word to report invalid permeability). */
+ * returns DGPU_INVALID_INPUT). No context is needed and nothing is allocated;
+ * each call looks up the array's device address on the current device (the
+ * first call on a device loads the library's device code there). All calls
+ * share the one array, so calls that overlap on the GPU race; serialise them.
+ * The call is synchronous: it waits for the stream and reads back a status
+ * word (to report invalid permeability) before it returns, so it must never
+ * be made on a stream that is being captured. */
 int dgpu_apply_preconditioner_noalloc(const double* d_a, const double* d_r, int64_t n, int pre_sweeps,
                                       int post_sweeps, int cycle_index, double* d_z, void* stream);
 
@@ -229,6 +231,14 @@ int dgpu_net_set_params(dgpu_net* net, const float* in);
 int dgpu_net_get_scaling(dgpu_net* net, double* out4);
 int dgpu_net_set_scaling(dgpu_net* net, const double* in4);
 int dgpu_net_set_engine(dgpu_net* net, int engine);
+/* Test hook (no counterpart in the reference): how many times each
+ * tensor-core convolution CTA polls its first MMA-completion mbarrier before
+ * declaring the wait lost (default and maximum 2^24). 0 makes that wait run
+ * out at once, so the timeout path can be exercised without a fault: the
+ * kernel records the error, drains the MMA in flight with the full budget,
+ * frees its tensor memory and returns, and the call reports DGPU_TIMEOUT.
+ * Pass 1 << 24 to restore the default. */
+int dgpu_net_set_first_wait(dgpu_net* net, long long polls);
 
 #define DGPU_NET_LOSS_ENERGY 0 /* e^T A e / u^T A u per sample, batch mean (default) */
 #define DGPU_NET_LOSS_MSE 1    /* mean of (u0 - u)^2 over all cells, u scaled to unit RMS */

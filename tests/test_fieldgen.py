@@ -78,7 +78,11 @@ def test_gpu_fields_validation(capi) -> None:
 
 
 @pytest.mark.gpu
-def test_dataset_command_writes_reference_format(capi, tmp_path) -> None:
+def test_dataset_command_writes_reference_format(capi, orc, tmp_path) -> None:
+    """The dataset command (python/darcy/cli.py:77-115): the reference's field
+    loop, npz(a, u) in float32, every u equal to the oracle's solution of its
+    field after the same float32 cast (rtol 1e-6: the GPU solve is within
+    ~1e-12 of the oracle's, so the casts differ by at most one float32 ulp)."""
     from darcy_cpp_gb300 import dataset
 
     out = tmp_path / "d.npz"
@@ -88,11 +92,11 @@ def test_dataset_command_writes_reference_format(capi, tmp_path) -> None:
         assert z["a"].shape == (6, 24, 24)
         # the reference's field loop: one shared stream
         assert np.array_equal(z["a"], dataset.draw_fields(6, 24, seed=4).astype(np.float32))
-    import darcy_cpp_gb300 as darcy
-
-    r = darcy.solve(dataset.draw_fields(6, 24, seed=4)[2])
+    fields = dataset.draw_fields(6, 24, seed=4)
     with np.load(out) as z:
-        assert np.allclose(z["u"][2], r.u.astype(np.float32), rtol=1e-6, atol=0)
+        for q in range(6):
+            want = orc.solve(fields[q], tol=1e-10)["u"]
+            assert np.allclose(z["u"][q], want.astype(np.float32), rtol=1e-6, atol=0), q
     gpu = tmp_path / "g.npz"
     assert dataset.main(["--n-samples", "4", "--grid", "24", "--gpu-fields", "--output", str(gpu)]) == 0
     with np.load(gpu) as z:

@@ -333,3 +333,32 @@ def test_network_validation(learn) -> None:
         learn.solve_batch_learned(net, np.ones((1, 64, 64)))
     with pytest.raises(capi.InvalidInput, match="learning rate"):
         net.handle.train(1, 1, lr=0.0)
+
+
+@pytest.mark.gpu
+def test_mma_wait_that_runs_out_reports_timeout_and_the_net_recovers(learn) -> None:
+    """The tensor-core convolution's bounded MMA-completion wait: with its
+    first wait given no polls (test hook), every CTA records the lost wait,
+    drains its MMA in flight with the full budget, frees its tensor memory and
+    returns; the call reports DGPU_TIMEOUT. The context stays usable: with the
+    default budget restored the prediction equals the one before, bit for bit,
+    and the solver still runs."""
+    from darcy_cpp_gb300 import capi
+
+    side = 32
+    net = learn.WarmStartNet(side, seed=7)
+    a = fields(side, range(3))
+    net.set_scaling([float(np.log(a).mean()), float(np.log(a).std()) or 1.0, 1e-2, 1.0])
+    net.set_params(np.random.default_rng(1).standard_normal(net.num_params).astype(np.float32) * 0.2)
+    before = net.predict(a)
+    net.handle.set_first_wait(0)
+    with pytest.raises(capi.DarcyGpuError, match=f"status {capi.TIMEOUT}: .*wait ran out"):
+        net.predict(a)
+    net.handle.set_first_wait(1 << 24)
+    after = net.predict(a)
+    assert np.array_equal(before, after)
+    with pytest.raises(capi.InvalidInput, match="polls"):
+        net.handle.set_first_wait(-1)
+    import darcy_cpp_gb300 as darcy
+
+    assert darcy.solve(a[0]).converged

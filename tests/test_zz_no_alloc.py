@@ -59,6 +59,25 @@ def test_noalloc_matches_the_allocating_entry_point(env, n) -> None:
         assert rel_l2(got, want) < REL, (n, call)
 
 
+def test_noalloc_more_sweeps_v_cycle_at_the_largest_side(env) -> None:
+    """pre/post sweeps and the cycle index go through the shared setup (the
+    dense tail is built with them): n = 128, 2 pre and 3 post sweeps, V-cycle,
+    twice in a row against the allocating entry point with the same options."""
+    torch, capi, ctx = env
+    n = 128
+    rng = np.random.default_rng(5)
+    for call in range(2):
+        a = two_phase(n, seed=40 + call, hi=1e2, lo=1e-2)
+        r = rng.standard_normal((n, n))
+        want = ctx.apply_preconditioner(a, r, pre_sweeps=2, post_sweeps=3, cycle_index=1)
+        d_a, d_r = device(torch, a), device(torch, r)
+        d_z = torch.empty_like(d_r)
+        capi.apply_preconditioner_noalloc(d_a.data_ptr(), d_r.data_ptr(), n, d_z.data_ptr(), pre_sweeps=2,
+                                          post_sweeps=3, cycle_index=1,
+                                          stream=torch.cuda.current_stream().cuda_stream)
+        assert rel_l2(d_z.cpu().numpy(), want) < REL, call
+
+
 def test_noalloc_repeats_bit_for_bit(env) -> None:
     torch, capi, _ = env
     n = 48
