@@ -28,9 +28,10 @@ __device__ __forceinline__ double apply_cell(const Lvl64& L, const double* __res
 // wb/sb boundary vectors), the five FP64 CG vectors b, r, p, Ap, z, the
 // cycle's own coefficient copies and iterate/right-hand side for the large
 // levels, and the scratch used once per problem to build the dense tail.
-// Shared memory: the dense tail operator, then the cycle's data for as many
-// coarse levels as fit in `sbudget` bytes. Level 0 of an FP64 cycle works
-// directly on r (right-hand side) and z (iterate).
+// Shared memory: level 0's cycle data when all of it fits in `sbudget` bytes,
+// then the dense tail operator, then the cycle's data for as many coarse
+// levels as fit. Level 0 of an FP64 cycle works directly on r (right-hand
+// side) and z (iterate).
 //
 // Dense tail: the levels from tl (the first level of side <= kBlockTailSide,
 // when that is not level 0) down implement the fixed map "x = 0, then gamma
@@ -85,13 +86,21 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
         }
     const int ntail = tl ? sides[tl] * sides[tl] : 0;
     const int cyc_levels = tl ? tl : nlev;  // levels the cycle itself visits
-    // shared memory: the tail operator first, then the coarsest cycle levels that fit
-    // (the operator plus level tl's x and b, which it reads and writes)
-    size_t need = tl ? (((size_t)ntail * ntail * sizeof(T) + 15) & ~(size_t)15) +
-                           2 * (((size_t)ntail * sizeof(T) + 15) & ~(size_t)15)
-                     : 0;
-    const bool tail_shared = tl && need <= sbudget;
-    if (!tail_shared) need = 0;
+    const bool fp32 = sizeof(T) == 4;
+    // Shared memory, in order of the traffic it saves: level 0's cycle data
+    // when the whole of it fits (a visit of level l moves ~4^-l of level 0's
+    // bytes and happens 2^l times per W-cycle, so level 0 carries about half
+    // of a cycle's traffic: the coefficient copies, and for an FP32 cycle its
+    // iterate and right-hand side too); then the tail operator (with level
+    // tl's x and b, which it reads and writes); then the coarsest cycle levels
+    // that still fit.
+    auto arr = [](size_t cells) { return ((cells * sizeof(T) + 15) & ~(size_t)15); };
+    const size_t l0_bytes = (fp32 ? 6 : 4) * arr((size_t)n * n);
+    const bool l0_shared = nlev > 1 && cyc_levels >= 1 && l0_bytes <= sbudget;
+    size_t need = l0_shared ? l0_bytes : 0;
+    const size_t tail_bytes = tl ? arr((size_t)ntail * ntail) + 2 * arr((size_t)ntail) : 0;
+    const bool tail_shared = tl && need + tail_bytes <= sbudget;
+    if (tail_shared) need += tail_bytes;
     int ls = cyc_levels;
     for (int l = cyc_levels - 1; l >= 1; --l) {
         const size_t lvl = 6 * (((size_t)sides[l] * sides[l] * sizeof(T) + 15) & ~(size_t)15);
@@ -110,7 +119,6 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
                                  : gtake(sizeof(T) * (size_t)ntail * ntail));
         if (v) v->tail = tp;
     }
-    const bool fp32 = sizeof(T) == 4;
     const size_t m0 = (size_t)n * n;
     for (int l = 0; l < nlev; ++l) {
         const size_t m = (size_t)sides[l] * sides[l];
@@ -136,7 +144,7 @@ __host__ __device__ BlockLayout carve(int n, char* gbase, char* sbase, size_t sb
             if (v) v->lv[l] = V;
             continue;
         }
-        const bool shared = (l >= ls && l < cyc_levels) || (tail_shared && l == tl);
+        const bool shared = (l == 0 && l0_shared) || (l >= ls && l < cyc_levels) || (tail_shared && l == tl);
         auto take = [&](size_t bytes) { return shared ? stake(bytes) : gtake(bytes); };
         if (l < cyc_levels) {
             if (fp32 || shared) {

@@ -263,6 +263,7 @@ struct dgpu_context {
     std::vector<cudaStream_t> slot_streams;
     std::vector<cudaEvent_t> slot_events;
     std::map<PlanKey, std::unique_ptr<GridPlan>> slot_plans;
+    std::vector<PlanKey> slot_families;  // families with slot plans, least recently used first
 };
 
 namespace {
@@ -862,6 +863,9 @@ bool route_to_grid(const dgpu_context* C, int64_t n, int64_t total_cells) {
     return n >= kGridEngineMinSide && n * n > total_cells / (2 * (int64_t)std::max(C->sms, 1));
 }
 
+// Problem families (side, form, options) whose slot plans stay allocated.
+constexpr size_t kSlotFamilies = 4;
+
 // Concurrent slots for grid_solve_many (DARCY_GPU_SLOTS overrides, 1..16).
 int grid_slots() {
     const char* e = std::getenv("DARCY_GPU_SLOTS");
@@ -894,13 +898,30 @@ float grid_solve_many(dgpu_context* C, int side, const std::vector<int64_t>& ord
             C->slot_events.push_back(ev);
         }
     }
-    // slot plans of one problem family at a time (they hold O(n^2) memory each)
+    // slot plans of up to kSlotFamilies problem families (they hold O(n^2)
+    // memory each), the least recently used family evicted first: rebuilding a
+    // family's plans and graphs costs ~1.5 ms a slot at 1024^2, which a caller
+    // alternating between two forms would otherwise pay on every call
     PlanKey K{side, o->form, o->preconditioner, o->pre_sweeps, o->post_sweeps, o->cycle_index, f != nullptr,
               u0 != nullptr};
-    if (!C->slot_plans.empty()) {
-        PlanKey k0 = C->slot_plans.begin()->first;
-        k0.slot = 0;
-        if (k0 < K || K < k0) C->slot_plans.clear();
+    {
+        auto same = [](const PlanKey& x, const PlanKey& y) { return !(x < y) && !(y < x); };
+        auto& lru = C->slot_families;  // most recent last
+        for (auto it = lru.begin(); it != lru.end(); ++it)
+            if (same(*it, K)) {
+                lru.erase(it);
+                break;
+            }
+        lru.push_back(K);
+        while (lru.size() > kSlotFamilies) {
+            const PlanKey old = lru.front();
+            lru.erase(lru.begin());
+            for (auto it = C->slot_plans.begin(); it != C->slot_plans.end();) {
+                PlanKey k0 = it->first;
+                k0.slot = 0;
+                it = same(k0, old) ? C->slot_plans.erase(it) : std::next(it);
+            }
+        }
     }
     std::vector<GridPlan*> plans((size_t)S);
     for (int q = 0; q < S; ++q) {
@@ -1064,6 +1085,11 @@ size_t smem_budget_for(bool mixed) { return mixed ? 48 * 1024 : 96 * 1024; }
 // level and the tail on chip, one CTA per SM): then only the FP64 CG vectors
 // and fine-level coefficients live in global memory.
 constexpr size_t kSmemBudgetLarge = 180 * 1024;
+// Level 0 of a 64^2 FP32 cycle alone (6 x 16 KiB), two CTAs of up to 512
+// threads per SM: the cycle's heaviest level on chip, and the FP64 CG vectors
+// and coefficients of the two resident problems per SM (~300 KB each) within
+// the L2.
+constexpr size_t kSmemBudgetLevel0 = 100 * 1024;
 
 // Autotuning key of a batch (loads the tuning file on first use). Batches
 // too small to put 4 problems on every SM ("few") tune apart from larger ones
@@ -1233,6 +1259,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
             add(threads, smem_budget_for(mixed));
             if (threads == 1024) add(threads, 96 * 1024);
             if (mixed && threads >= 512) add(threads, kSmemBudgetLarge);
+            if (mixed && threads >= 256 && threads <= 512) add(threads, kSmemBudgetLevel0);
         }
         // Time budget: each candidate costs three launches over the sample,
         // and a launch lasts as long as its largest problem's single-CTA solve

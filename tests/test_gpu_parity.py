@@ -629,6 +629,33 @@ def test_batched_engine_takes_any_whole_warp_count(darcy, monkeypatch, tmp_path,
         assert rel_l2(got["u"][q], want["u"][q]) < REL_L2
 
 
+@pytest.mark.parametrize("threads", [256, 512])
+@pytest.mark.parametrize("n", [64, 57])
+def test_level0_of_the_fp32_cycle_in_shared_memory_is_bit_identical(darcy, monkeypatch, tmp_path, threads,
+                                                                   n) -> None:
+    """A shared-memory budget that holds level 0 of the FP32 cycle (its six
+    arrays) moves it on chip: the same arithmetic in the same order as with
+    level 0 in global memory (same thread count, so the same reductions), so
+    the same bits."""
+    import json
+
+    import torch
+    from darcy_cpp_gb300 import capi
+
+    batch_a = np.stack([two_phase(n, seed=s, hi=1e2, lo=1e-2) for s in range(5)])
+    key = f"{torch.cuda.get_device_name(0)}|side<=64|mixed|pc2|c2|s11|few"
+    out = {}
+    for budget in (16384, 100 * 1024):
+        tune = tmp_path / f"tune{budget}.json"
+        tune.write_text(json.dumps({key: [threads, budget]}))
+        monkeypatch.setenv("DARCY_GPU_TUNE_FILE", str(tune))
+        out[budget] = capi.Context().solve_batch(batch_a, form="mixed")
+    a, b = out[16384], out[100 * 1024]
+    assert b["converged"].all()
+    assert np.array_equal(a["iterations"], b["iterations"])
+    assert np.array_equal(a["u"], b["u"])
+
+
 def test_tuning_file_shapes_the_kernel_cannot_take_are_ignored(darcy, monkeypatch, tmp_path) -> None:
     import json
 
