@@ -24,7 +24,7 @@ The compact figures of every workload are repeated as the last key
 (`summary`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-    python bench.py --profile {solve,batch,net,kernels} [--n N] [--form F] [--reps R] ...
+    python bench.py --profile {solve,batch,net,kernels,predict} [--n N] [--form F] [--reps R] ...
 
 `--impl reference` times the reference itself -- its own Python package and
 C++ extension (baseline/_ref, installed and compiled by oracle/build_ref.py)
@@ -814,7 +814,9 @@ def profile(args) -> int:
     * `kernels`: each kernel of one CG iteration timed back to back
       (dgpu_profile_kernels), launched directly on the stream;
     * `batch`: the batched solve of --count problems of side --n;
-    * `net`: a few training steps of the warm-start network, then one prediction.
+    * `net`: a few training steps of the warm-start network, then one prediction;
+    * `predict`: --reps predictions of --count fields of side --side by a network
+      with random weights (inference kernels only, no training launches).
     """
     if args.profile in ("solve", "kernels") and not args.device_loop:
         os.environ.setdefault("DARCY_GPU_LOOP", "host")
@@ -844,6 +846,19 @@ def profile(args) -> int:
             dt = time.perf_counter() - t0
         print(f"batch {args.count} x {args.n}^2 form={args.form}: {args.count / dt:.0f} solves/s, "
               f"mean {r.iterations.mean():.1f} iterations")
+    elif args.profile == "predict":
+        from darcy_cpp_gb300 import learn
+
+        a = np.stack([field(args.side, s, 12.0, 3.0) for s in range(args.count)])
+        net = learn.WarmStartNet(args.side, seed=0)
+        net.set_scaling([float(np.log(a).mean()), float(np.log(a).std()), 1e-2, 1.0])
+        net.set_params(np.random.default_rng(0).standard_normal(net.num_params).astype(np.float32) * 0.1)
+        for _ in range(args.reps):
+            t0 = time.perf_counter()
+            u0 = net.predict(a)
+            dt = time.perf_counter() - t0
+        print(f"predict side={args.side} count={args.count}: {dt * 1e6 / args.count:.2f} us per field "
+              f"(host arrays), {u0.shape}")
     else:
         from darcy_cpp_gb300 import learn
 
@@ -862,7 +877,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     prof = ap.add_argument_group("profiling driver")
-    prof.add_argument("--profile", choices=["solve", "batch", "net", "kernels"])
+    prof.add_argument("--profile", choices=["solve", "batch", "net", "kernels", "predict"])
     prof.add_argument("--n", type=int, default=1024)
     prof.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     prof.add_argument("--reps", type=int, default=2)

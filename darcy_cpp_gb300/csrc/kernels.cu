@@ -995,6 +995,17 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             sr += rk * rk;
         }
         residual = sqrt(block_sum_wide(sr, red)) / bnorm;
+        // A predicted start no better than zero (||b - A u0|| >= ||b||) is
+        // dropped for the zero start, the fallback it is judged against: CG
+        // from it would need more iterations to reach the same tolerance.
+        if (A.u0_fallback && !(residual < 1.0)) {
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+                u[k] = 0.0;
+                r[k] = b[k];
+            }
+            residual = 1.0;
+            __syncthreads();
+        }
     } else {
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) r[k] = b[k];
         residual = 1.0;

@@ -1192,6 +1192,7 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         double* d_u0 = C->bu0.ensure(total);
         (*warm)(A.a, d_u0, s);
         A.u0 = d_u0;
+        A.u0_fallback = 1;
     }
     CK(cudaMemcpyAsync((void*)A.order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync((void*)A.side, sides.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));

@@ -362,3 +362,28 @@ def test_mma_wait_that_runs_out_reports_timeout_and_the_net_recovers(learn) -> N
     import darcy_cpp_gb300 as darcy
 
     assert darcy.solve(a[0]).converged
+
+
+@pytest.mark.gpu
+def test_learned_start_no_better_than_zero_falls_back_to_zero(learn) -> None:
+    """A predicted start whose residual is not below ||b|| is replaced by the
+    zero start in the batched solve (the fallback it is judged against):
+    with predictions ~1e3 times too large, every problem takes the zero
+    start's iterations and ends at its solution."""
+    import darcy_cpp_gb300 as darcy
+
+    side = 32
+    a = fields(side, range(6))
+    net = learn.WarmStartNet(side, seed=5)
+    net.set_scaling([float(np.log(a).mean()), float(np.log(a).std()) or 1.0, 1e3, 1.0])
+    net.set_params(np.random.default_rng(2).standard_normal(net.num_params).astype(np.float32) * 0.2)
+    u0 = net.predict(a)
+    b = np.full((side, side), 1.0 / (side + 1) ** 2)
+    for q in range(len(a)):
+        assert np.linalg.norm(b - darcy.apply_operator(a[q], u0[q])) > np.linalg.norm(b)
+    warm = learn.solve_batch_learned(net, a, tol=1e-10, form="mixed")
+    zero = darcy.solve_batch(a, tol=1e-10, form="mixed")
+    assert warm.all_converged
+    assert np.array_equal(warm.iterations, zero.iterations)
+    for q in range(len(a)):
+        assert rel_l2(warm.u[q], zero.u[q]) < 1e-12
