@@ -759,8 +759,11 @@ def run_combined(fields: list[np.ndarray], pairs: tuple[np.ndarray, np.ndarray],
     for form in ("mixed", "fp64"):
         darcy.solve_batch_uneven(fields, tol=TOL, form=form)  # launch shape tuned, untimed
         sec, r = best_of(lambda form=form: darcy.solve_batch_uneven(fields, tol=TOL, form=form), 2, flush)
-        # per-size cost from each size alone (one call per size, same form)
+        # per-size cost from each size alone (one call per size, same form; the
+        # first call of each tunes its launch shape, untimed)
+        darcy.solve_batch(small, tol=TOL, form=form)
         s_small, _ = best_of(lambda form=form: darcy.solve_batch(small, tol=TOL, form=form), 1, flush)
+        darcy.solve_batch_uneven(big, tol=TOL, form=form)
         s_big, _ = best_of(lambda form=form: darcy.solve_batch_uneven(big, tol=TOL, form=form), 1, flush)
         out[form] = {"solves_per_s": round(total / sec, 1), "seconds": round(sec, 4),
                      "mean_iterations_128": round(float(r.iterations[:COMB_SMALL].mean()), 3),

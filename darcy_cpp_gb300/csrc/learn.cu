@@ -71,6 +71,7 @@ typedef __nv_bfloat16 bf16;
 // strided run of staged positions, shifted by dy * P + dx.
 struct Geom {
     int H, W, P, tiles_per_img, nq;  // nq: staged positions per tile (multiple of 8)
+    int step_r, step_c;              // kTile positions = step_r rows + step_c columns of pitch P
 };
 
 inline bool side_supported(int s) { return s >= 8 && s <= kMaxSide && (s % 2) == 0; }
@@ -81,12 +82,14 @@ inline Geom make_geom(int side) {
     g.P = side + 2;
     g.tiles_per_img = (side * g.P + kTile - 1) / kTile;
     g.nq = ((kTile + 2 * g.P + 2) + 7) & ~7;
+    g.step_r = kTile / g.P;
+    g.step_c = kTile % g.P;
     return g;
 }
 
 // Tile t -> first pixel of its image and first padded position.
 __device__ __forceinline__ void tile_origin(int64_t t, const Geom& g, int64_t& pbase, int& s0) {
-    const int64_t b = t / g.tiles_per_img;
+    const int64_t b = t < (1ll << 31) ? (int64_t)((int)t / g.tiles_per_img) : t / g.tiles_per_img;
     s0 = (int)(t - b * g.tiles_per_img) * kTile;
     pbase = b * (int64_t)g.H * g.W;
 }
@@ -97,6 +100,30 @@ __device__ __forceinline__ int position_pixel(const Geom& g, int s) {
     const int r = s / g.P, c = s - r * g.P;
     if (r >= g.H || c < 1 || c > g.W) return -1;
     return r * g.W + c - 1;
+}
+
+// Padded position s >= -2P as (row, column) of pitch P (rows of negative
+// positions are negative), with one division; stepping by rows and columns
+// after that needs none.
+struct PosRC {
+    int r, c;
+};
+__device__ __forceinline__ PosRC position_rc(const Geom& g, int s) {
+    const int t = s + 2 * g.P;
+    const int r = t / g.P;
+    return PosRC{r - 2, t - r * g.P};
+}
+__device__ __forceinline__ PosRC rc_add(const Geom& g, PosRC p, int dr, int dc) {
+    p.r += dr;
+    p.c += dc;
+    if (p.c >= g.P) {
+        p.c -= g.P;
+        p.r += 1;
+    }
+    return p;
+}
+__device__ __forceinline__ int rc_pixel(const Geom& g, PosRC p) {
+    return (p.r >= 0 && p.r < g.H && p.c >= 1 && p.c <= g.W) ? p.r * g.W + p.c - 1 : -1;
 }
 
 // ------------------------------------------------------------ elementwise
@@ -464,11 +491,13 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
 template <int CCH>
 __device__ __forceinline__ void stage_tile(const bf16* __restrict__ x, const Geom& g, int64_t pbase, int s0,
                                            uint32_t buf, uint32_t plane) {
-    for (int t = threadIdx.x; t < CCH * g.nq; t += kConvThreads) {
-        const int c = t / g.nq, q = t - c * g.nq;
-        const int pix = position_pixel(g, s0 - g.P - 1 + q);
-        const bf16* src = pix >= 0 ? x + ((pbase + pix) * CCH + c) * 8 : x;
-        cp_async16(buf + c * plane + q * 16, src, pix >= 0);
+    PosRC pos = position_rc(g, s0 - g.P - 1 + (int)threadIdx.x);
+    for (int q = threadIdx.x; q < g.nq; q += kConvThreads) {
+        const int pix = rc_pixel(g, pos);
+        const bf16* src = pix >= 0 ? x + (pbase + pix) * CCH * 8 : x;
+#pragma unroll
+        for (int c = 0; c < CCH; ++c) cp_async16(buf + c * plane + q * 16, src + c * 8, pix >= 0);
+        pos = rc_add(g, pos, g.step_r, g.step_c);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
@@ -767,40 +796,44 @@ __host__ __device__ constexpr uint32_t mma_idesc_mn(int M, int N) {
     return mma_idesc(M, N) | (1u << 15) | (1u << 16);
 }
 
+constexpr int kWgThreads = 2 * kTile;  // two threads per staged position: each stages half the planes
+
 template <int CCH, int NOUT, int CIN, int COUT, class TDY>
 __device__ __forceinline__ void wgrad_stage(const bf16* __restrict__ x, const TDY* __restrict__ dy, const Geom& g,
                                             int64_t pbase, int s0, unsigned char* buf) {
     using W = WgradTc<CCH, NOUT>;
-    const int q = threadIdx.x;  // one position of the tile per thread (kConvThreads == kTile)
+    const int q = threadIdx.x & (kTile - 1), half = threadIdx.x / kTile;
     const uint32_t a = smem_u32(buf);
+    const PosRC base = position_rc(g, s0 - g.P - 1 + q);  // tap (0, 0) of output position s0 + q
 #pragma unroll 1
-    for (int pl = 0; pl < W::kDataPlanes; ++pl) {
+    for (int pl = half; pl < W::kDataPlanes; pl += 2) {
         const int tap = pl / CCH, c = pl - tap * CCH;
-        const int pix = position_pixel(g, s0 - g.P - 1 + q + (tap / 3) * g.P + tap % 3);
+        const int pix = rc_pixel(g, rc_add(g, base, tap / 3, tap % 3));
         const bf16* src = pix >= 0 ? x + ((pbase + pix) * CCH + c) * 8 : x;
         asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(a + pl * W::kPlane + q * 16), "l"(src),
                      "r"(pix >= 0 ? 16 : 0)
                      : "memory");
     }
-    const int pix = position_pixel(g, s0 + q);
+    const int pix = rc_pixel(g, rc_add(g, base, 1, 1));  // output position s0 + q
     const uint32_t b = a + W::kAPlanes * W::kPlane;
     if constexpr (sizeof(TDY) == 2) {
 #pragma unroll
-        for (int c = 0; c < W::kBPlanes; ++c) {
+        for (int c = half; c < W::kBPlanes; c += 2) {
             const TDY* src = pix >= 0 ? dy + (pbase + pix) * COUT + c * 8 : dy;
             asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(b + c * W::kPlane + q * 16),
                          "l"(src), "r"(pix >= 0 ? 16 : 0)
                          : "memory");
         }
-    } else {  // one FP32 channel -> BF16 hi in column 0, lo in column 1
+    } else if (half == 0) {  // one FP32 channel -> BF16 hi in column 0, lo in column 1
         const float d = pix >= 0 ? to_f(dy[pbase + pix]) : 0.f;
         const bf16 hi = __float2bfloat16(d);
         const bf16 lo = __float2bfloat16(d - __bfloat162float(hi));
         __nv_bfloat162 pr;
         pr.x = hi;
         pr.y = lo;
-        uint4 row = make_uint4(*reinterpret_cast<const uint32_t*>(&pr), 0u, 0u, 0u);
-        *reinterpret_cast<uint4*>(buf + W::kAPlanes * W::kPlane + q * 16) = row;
+        *reinterpret_cast<uint4*>(buf + W::kAPlanes * W::kPlane + q * 16) =
+            make_uint4(*reinterpret_cast<const uint32_t*>(&pr), 0u, 0u, 0u);
+    } else {
 #pragma unroll
         for (int c = 1; c < W::kBPlanes; ++c)
             *reinterpret_cast<uint4*>(buf + (W::kAPlanes + c) * W::kPlane + q * 16) = make_uint4(0u, 0u, 0u, 0u);
@@ -809,11 +842,10 @@ __device__ __forceinline__ void wgrad_stage(const bf16* __restrict__ x, const TD
 }
 
 template <int CCH, int NOUT, int CIN, int COUT, class TDY>
-__global__ void __launch_bounds__(kConvThreads) k_wgrad_tc(const bf16* __restrict__ x, const TDY* __restrict__ dy,
+__global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const bf16* __restrict__ x, const TDY* __restrict__ dy,
                                                            Geom g, int64_t ntiles, float* __restrict__ part,
                                                            int* __restrict__ err, long long first_wait) {
     using W = WgradTc<CCH, NOUT>;
-    static_assert(kConvThreads == kTile, "one staged position per thread");
     constexpr int K = kTaps * CIN;
     constexpr int NV = (K + 1) * COUT;
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -824,9 +856,10 @@ __global__ void __launch_bounds__(kConvThreads) k_wgrad_tc(const bf16* __restric
     // constant planes of both stages: the ones plane (bias row) and zeros up
     // to the M tile boundary; staging never writes them
     for (int st = 0; st < 2; ++st)
-        for (int pl = W::kDataPlanes; pl < W::kAPlanes; ++pl) {
+        for (int pl = W::kDataPlanes + tid / kTile; pl < W::kAPlanes; pl += kWgThreads / kTile) {
             const uint32_t one = pl == W::kDataPlanes ? 0x3F803F80u : 0u;  // BF16 1.0 pairs
-            *reinterpret_cast<uint4*>(sm + st * W::kStage + pl * W::kPlane + tid * 16) = make_uint4(one, one, one, one);
+            *reinterpret_cast<uint4*>(sm + st * W::kStage + pl * W::kPlane + (tid & (kTile - 1)) * 16) =
+                make_uint4(one, one, one, one);
         }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -901,11 +934,14 @@ __global__ void __launch_bounds__(kConvThreads) k_wgrad_tc(const bf16* __restric
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (any && !failed) {
         float* out = part + (int64_t)blockIdx.x * NV;
-        const int r = warp * 32 + lane;  // row of D (tensor-memory lane)
+        // warp w reads tensor-memory lanes 32 (w % 4) .. + 31; the two groups of
+        // four warps take alternate M tiles
+        const int sub = warp & 3, group = warp >> 2;
+        const int r = sub * 32 + lane;  // row of D (tensor-memory lane)
 #pragma unroll 1
-        for (int mt = 0; mt < W::MT; ++mt) {
+        for (int mt = group; mt < W::MT; mt += kWgThreads / 128) {
             float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + mt * NOUT, v);
+            tmem_ld32(tmem + ((uint32_t)(sub * 32) << 16) + mt * NOUT, v);
             const int pl = mt * 16 + r / 8, e = r % 8;
             int k = -1;
             if (pl < W::kDataPlanes) {
@@ -1224,7 +1260,7 @@ void wgrad(dgpu_net* N, const bf16* x, const TDY* dy, int64_t count, int layer) 
         NCK(cudaFuncSetAttribute(k_wgrad_tc<CCH, NOUT, CIN, COUT, TDY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  W::kSmem));
         ctas = (int)std::min<int64_t>(ntiles, N->sms);
-        k_wgrad_tc<CCH, NOUT, CIN, COUT, TDY><<<ctas, kConvThreads, W::kSmem, N->stream>>>(
+        k_wgrad_tc<CCH, NOUT, CIN, COUT, TDY><<<ctas, kWgThreads, W::kSmem, N->stream>>>(
             x, dy, N->g, ntiles, N->gpart.p, N->err.p, N->first_wait);
     } else {
         ctas = (int)std::min<int64_t>(ntiles, N->wg_ctas);

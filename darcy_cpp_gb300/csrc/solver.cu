@@ -1262,6 +1262,10 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
             if (mixed && threads >= 512) add(threads, kSmemBudgetLarge);
             if (mixed && threads >= 256 && threads <= 512) add(threads, kSmemBudgetLevel0);
         }
+        // odd warp counts between the powers of two: 5-6 CTAs of 192 threads or
+        // 2-3 of 384 per SM, with a smaller coarse-level budget so that they fit
+        for (int threads : {192, 256, 384}) add(threads, 32 * 1024);
+        for (int threads : {192, 384}) add(threads, smem_budget_for(mixed));
         // Time budget: each candidate costs three launches over the sample,
         // and a launch lasts as long as its largest problem's single-CTA solve
         // (over a second for 512^2). When the default's launch exceeds
