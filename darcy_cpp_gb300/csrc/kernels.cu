@@ -1022,8 +1022,13 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         double rz = block_precondition<T>(A, V, r, z, red);
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k];
         __syncthreads();
+        // Even sides take the paired loops: two cells per thread, 16-byte
+        // FP64 accesses (arena vectors are 256-byte aligned; u also needs an
+        // even offset in the packed output).
+        const bool pairs = (n & 1) == 0;
+        const bool pairs_u = pairs && (((uintptr_t)u) & 15) == 0;
         for (int it = 0; it < A.max_iter; ++it) {
-            const double pap = block_apply_dot(h[0], p, ap, red);
+            const double pap = pairs ? block_apply_dot2(h[0], p, ap, red) : block_apply_dot(h[0], p, ap, red);
             if (!(fabs(pap) > 0.0) || !isfinite(pap)) {
                 iterations = it;
                 converged = 0;
@@ -1034,13 +1039,36 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             // the FP32 cycle's input (r rounded) is written here, in the same pass
             const bool round_b = sizeof(T) == 4 && A.pc == kPcMultigrid;
             T* b32 = V.lv[0].b;
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-                u[k] += alpha * p[k];
-                const double rk = r[k] - alpha * ap[k];
-                r[k] = rk;
-                rr += rk * rk;
-                if (round_b) b32[k] = narrow_to<T>(rk);
-                if (flexible) rzo += rk * z[k];  // z still holds the previous direction's z
+            if (pairs_u && !flexible) {
+                double2* u2 = reinterpret_cast<double2*>(u);
+                double2* r2 = reinterpret_cast<double2*>(r);
+                const double2* p2 = reinterpret_cast<const double2*>(p);
+                const double2* a2 = reinterpret_cast<const double2*>(ap);
+                for (int64_t q = threadIdx.x; q < (m >> 1); q += blockDim.x) {
+                    double2 uu = u2[q], rv = r2[q];
+                    const double2 pp = p2[q], av = a2[q];
+                    uu.x += alpha * pp.x;
+                    uu.y += alpha * pp.y;
+                    rv.x = rv.x - alpha * av.x;
+                    rv.y = rv.y - alpha * av.y;
+                    u2[q] = uu;
+                    r2[q] = rv;
+                    rr += rv.x * rv.x;
+                    rr += rv.y * rv.y;
+                    if (round_b) {
+                        b32[2 * q] = narrow_to<T>(rv.x);
+                        b32[2 * q + 1] = narrow_to<T>(rv.y);
+                    }
+                }
+            } else {
+                for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+                    u[k] += alpha * p[k];
+                    const double rk = r[k] - alpha * ap[k];
+                    r[k] = rk;
+                    rr += rk * rk;
+                    if (round_b) b32[k] = narrow_to<T>(rk);
+                    if (flexible) rzo += rk * z[k];  // z still holds the previous direction's z
+                }
             }
             residual = sqrt(block_sum_wide(rr, red)) / bnorm;
             if (flexible) rzo = block_sum_wide(rzo, red);
@@ -1053,7 +1081,19 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
             const double rz_new = block_precondition<T>(A, V, r, z, red, round_b);
             const double beta = (rz_new - rzo) / rz;
             rz = rz_new;
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k] + beta * p[k];
+            if (pairs) {
+                double2* p2 = reinterpret_cast<double2*>(p);
+                const double2* z2 = reinterpret_cast<const double2*>(z);
+                for (int64_t q = threadIdx.x; q < (m >> 1); q += blockDim.x) {
+                    const double2 zz = z2[q];
+                    double2 pp = p2[q];
+                    pp.x = zz.x + beta * pp.x;
+                    pp.y = zz.y + beta * pp.y;
+                    p2[q] = pp;
+                }
+            } else {
+                for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k] + beta * p[k];
+            }
             __syncthreads();
         }
     }

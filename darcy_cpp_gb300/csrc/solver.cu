@@ -61,19 +61,18 @@ struct Failure {
 // slower at 1024^2: 44.5 against 38.9 ms, its 4096-column setup and 64 MB
 // products outweighing the launches it saves.)
 constexpr int kTailSide = 32;
-// Batch routing between the engines. A problem of side >= kGridEngineSide
+// Batch routing between the engines. A problem of side >= kGridEngineMinSide
 // goes to the grid engine, several such solves at once on their own streams
-// (grid_solve_many), after the block engine has run the rest. A problem of
-// side >= kGridEngineMinSide goes there too when it is more work than one
-// CTA's share of the batch (its cells > all cells / (2 x SMs)): on one CTA it
-// would outlast the rest, while beside many smaller problems it is hidden.
-// Measured on GB300 (device-resident, FP64 / mixed): 64 x 384^2 at contrast
-// 1e4, 481 / 553 ms on the block engine, 199 / 177 ms on the grid engine;
-// 64 x 512^2, 1097 / 1188 against 373 / 307 ms; 128 x 256^2 at contrast 4,
-// 71 / 55 against 182 / 140 ms (hence the lower bound); 16384 x 128^2 +
-// 64 x 512^2, 1423 / 1252 ms with the 512^2 problems in the block launch,
-// 1659 / 1344 ms with them routed (hence the share rule).
-constexpr int kGridEngineSide = 768;
+// (grid_solve_many), after the block engine has run the rest: on one CTA it
+// would outlast the rest of the batch, and beside many smaller problems it
+// would also set the block launch's shape (the autotuner keys on the largest
+// side: 1024 threads and one problem per SM for sides >= 256), which the
+// small problems then run with. Measured on GB300 (FP64 / mixed): 64 x 384^2
+// at contrast 1e4, 481 / 553 ms on the block engine against 199 / 177 ms on
+// the grid engine; 64 x 512^2, 1097 / 1188 against 373 / 307 ms; 128 x 256^2
+// at contrast 4, 71 / 55 against 182 / 140 ms (hence the lower bound);
+// 16384 x 128^2 + 64 x 512^2 end to end, 1.64 / 1.29 s with the 512^2
+// problems in the block launch against 1.49-1.62 / 1.10 s routed.
 constexpr int kGridEngineMinSide = 384;
 // Grid-engine levels of at least this side run the unfused kernels (see
 // emit_visit_hybrid); smaller ones the fused visits. Measured on GB300
@@ -859,8 +858,9 @@ bool route_to_grid(const dgpu_context* C, int64_t n, int64_t total_cells) {
     const char* e = std::getenv("DARCY_GPU_GRID_SIDE");
     const int v = e ? std::atoi(e) : 0;
     if (v >= 1) return n >= v;
-    if (n >= kGridEngineSide) return true;
-    return n >= kGridEngineMinSide && n * n > total_cells / (2 * (int64_t)std::max(C->sms, 1));
+    (void)C;
+    (void)total_cells;
+    return n >= kGridEngineMinSide;
 }
 
 // Problem families (side, form, options) whose slot plans stay allocated.
