@@ -51,7 +51,7 @@ struct BatchArgs {
     double fscalar;
     int f_shared;               // f is one n*n array shared by every problem
     const double* u0;           // packed warm start, or null
-    int u0_fallback;            // a warm start whose residual is not below ||b|| is replaced by zero
+    int u0_fallback;            // a warm start no better than zero in estimated energy norm is replaced by zero
     double* u;                  // packed solution (device)
     int* iterations;
     double* residual;

@@ -986,26 +986,18 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         return;
     }
 
+    double bu0 = 0.0;  // b . u0: estimates the solution's energy ||u||_A^2 = b . u for a close u0
     if (u0) {
-        double sr = 0.0;
+        double sr = 0.0, sbu = 0.0;
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
             const int i = (int)k / n, j = (int)k - i * n;  // n^2 < 2^31
             const double rk = b[k] - apply_cell(h[0], u, i, j);
             r[k] = rk;
             sr += rk * rk;
+            sbu += b[k] * u[k];
         }
         residual = sqrt(block_sum_wide(sr, red)) / bnorm;
-        // A predicted start no better than zero (||b - A u0|| >= ||b||) is
-        // dropped for the zero start, the fallback it is judged against: CG
-        // from it would need more iterations to reach the same tolerance.
-        if (A.u0_fallback && !(residual < 1.0)) {
-            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
-                u[k] = 0.0;
-                r[k] = b[k];
-            }
-            residual = 1.0;
-            __syncthreads();
-        }
+        if (A.u0_fallback) bu0 = block_sum_wide(sbu, red);
     } else {
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) r[k] = b[k];
         residual = 1.0;
@@ -1020,6 +1012,21 @@ __device__ void block_solve_one(const BatchArgs& A, int pid, const BlockViews<T>
         // no FP64 z array, measured 2% slower: 4096 x 64^2 mixed 23.1 against
         // 22.7 ms.)
         double rz = block_precondition<T>(A, V, r, z, red);
+        // A predicted start no better than zero is dropped for the zero start,
+        // the fallback it is judged against. CG minimises the error's energy
+        // norm; r0 . M r0 (the first preconditioned residual, computed here
+        // anyway) estimates the start's ||u - u0||_A^2 and b . u0 the
+        // solution's ||u||_A^2, so a start is kept while the first is below
+        // the second. A rejected start costs one more cycle (z = M b).
+        if (u0 && A.u0_fallback && !(rz < bu0)) {
+            for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+                u[k] = 0.0;
+                r[k] = b[k];
+            }
+            residual = 1.0;
+            __syncthreads();
+            rz = block_precondition<T>(A, V, r, z, red);
+        }
         for (int64_t k = threadIdx.x; k < m; k += blockDim.x) p[k] = z[k];
         __syncthreads();
         // Even sides take the paired loops: two cells per thread, 16-byte

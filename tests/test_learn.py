@@ -366,10 +366,11 @@ def test_mma_wait_that_runs_out_reports_timeout_and_the_net_recovers(learn) -> N
 
 @pytest.mark.gpu
 def test_learned_start_no_better_than_zero_falls_back_to_zero(learn) -> None:
-    """A predicted start whose residual is not below ||b|| is replaced by the
-    zero start in the batched solve (the fallback it is judged against):
-    with predictions ~1e3 times too large, every problem takes the zero
-    start's iterations and ends at its solution."""
+    """A predicted start no better than zero is replaced by the zero start in
+    the batched solve (the fallback it is judged against; the test is the
+    start's estimated energy-norm error r0 . M r0 against the solution's
+    estimated energy b . u0): with predictions ~1e3 times too large, every
+    problem takes the zero start's iterations and ends at its solution."""
     import darcy_cpp_gb300 as darcy
 
     side = 32
