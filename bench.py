@@ -536,7 +536,6 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         # ---- uneven batch and combined workload (end to end, host arrays)
         uneven_res = run_uneven(uneven, flush)
         comb_res = run_combined(comb, learn128, flush)
-    cpu = cpu_samples(CpuReference(), list(bigs), batch, uneven, comb)
 
     total_ms = {k: sum(v) for k, v in arms.items()}
     names = sorted(total_ms)
@@ -549,6 +548,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     e2e_slowest = {"mixed_batch": slowest[len(names) + 4], "fp64_serial": slowest[len(names) + 5]}
     if rank != 0:
         return None
+    # the reference on the host cores: rank 0 only (one set of samples per job)
+    cpu = cpu_samples(CpuReference(), list(bigs), batch, uneven, comb)
 
     # whole-job figures: the slowest replica's time over the solves of all replicas
     per_solve = {k: job_ms_per_solve(v, args.steps, nb, world) for k, v in total_ms.items()}
