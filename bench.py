@@ -12,6 +12,9 @@ fields; `e2e` is the chosen form through the package API from host arrays.
 gain (batched FP64, unbatched mixed) and the seed-1 field solved alone are
 reported beside it, and after the headline:
 
+* `single_2048`: the seed-1 field at 2048 x 2048 alone, both forms, and the
+  finest level's kernels at that size against the HBM copy peak;
+
 * `batch64`: 4096 problems of 64 x 64 (seeds 0..4095, {12, 3}), solves/s of
   both forms and of the learned warm start (the other half of the metric);
 * `uneven4096`: 4096 problems with sides drawn from {32, ..., 256} per seed;
@@ -57,6 +60,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "64² solves/s & 1024² ms/solve at rel-res 1e-10: chosen form vs plain FP64"
 N_BIG, SEED_BIG, HI_BIG, LO_BIG = 1024, 1, 1e3, 1e-3
 SEEDS_BIG = range(1, 9)  # the 1024 x 1024 workload: 8 fields, solved as one batch by the chosen form
+N_LARGE = 2048  # the large solves' second size: the seed-1 field alone, both forms
 WORKLOAD = ("1024x1024, 8 fields (GRF seeds 1..8), a in {1e3,1e-3}, f=1, W-cycle, tol 1e-10; "
             "chosen form solves them as one batch")
 N_SMALL, BATCH_SMALL = 64, 4096
@@ -416,6 +420,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     pool = FieldPool()
     try:
         bigs = np.stack(pool.make([(N_BIG, q, HI_BIG, LO_BIG) for q in SEEDS_BIG]))
+        large = pool.make([(N_LARGE, SEED_BIG, HI_BIG, LO_BIG)])[0]
         batch = np.stack(pool.make([(N_SMALL, s, 12.0, 3.0) for s in range(BATCH_SMALL)]))
         uneven = pool.make(uneven_specs())
         comb = pool.make(combined_specs())
@@ -510,6 +515,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             e2e["fp64_serial"].append(ms)
             e2e_res["fp64_serial"] = r
         torch.cuda.synchronize()
+        large_res = run_large(ctx, large, stream, timed, dev)
 
         # ---- 64 x 64 batch (the solves/s half of the metric)
         for form in ("mixed", "fp64"):  # launch shape tuned for the full batch, untimed
@@ -625,6 +631,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "single_seed1": single,
+        "single_2048": large_res,
         "batch64": b64,
         "uneven4096": {**uneven_res, "cpu_reference_solves_per_s": cpu["uneven4096_solves_per_s"]},
         "combined": {**comb_res, "cpu_reference": cpu["combined"]},
@@ -640,6 +647,8 @@ def summary_of(line: dict) -> dict:
         "1024_batch8_ms": {"chosen": line["value"], "plain_fp64": line["plain_fp64"]["value"],
                            "ratio": line["chosen_vs_plain"], "e2e": line["e2e"]["value"]},
         "1024_single_seed1_ms": {"mixed": s["mixed_ms"], "fp64": s["fp64_ms"], "ratio": s["fp64_over_mixed"]},
+        "2048_single_seed1_ms": {"mixed": line["single_2048"]["mixed_ms"], "fp64": line["single_2048"]["fp64_ms"],
+                                 "ratio": line["single_2048"]["fp64_over_mixed"]},
         "64_batch_solves_per_s": {"mixed": b["mixed"], "fp64": b["fp64"], "ratio": b["chosen_vs_plain"],
                                   "hbm_ratio": b["device_resident"]["chosen_vs_plain"],
                                   "learned": b["mixed_learned"], "cpu": b["cpu_reference"]},
@@ -675,6 +684,50 @@ def measure_roofline(ctx, a_big: np.ndarray, single_stats) -> dict:
                               "note": "shares from back-to-back launches of each kernel alone; the iteration "
                                       "from the seed-1 mixed solve's device time / iterations"},
             "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()} for p in prof]}
+
+
+def run_large(ctx, a: np.ndarray, stream, timed, dev: int) -> dict:
+    """The 2048 x 2048 seed-1 field alone, one solve per call on device
+    buffers (CUDA events, L2 flushed before each call, best of 2 after an
+    untimed call that builds the plan), both forms; and the kernels of a
+    mixed CG iteration that touch the finest level, timed back to back
+    against the HBM copy peak. The finest level's working set (~170 MB in
+    the mixed form) exceeds the 129 MB L2, but one kernel's own arrays may
+    not, and back-to-back launches of it then read part of them from L2
+    (a fraction above 1)."""
+    import torch
+
+    d_a = torch.from_numpy(a).to(f"cuda:{dev}")
+    d_u = torch.empty_like(d_a)
+    out, us = {}, {}
+    for form in ("mixed", "fp64"):
+        def call(form=form):
+            return ctx.solve_device(d_a.data_ptr(), N_LARGE, d_u.data_ptr(), stream.cuda_stream, tol=TOL, form=form)
+        call()
+        runs = [timed(call) for _ in range(2)]
+        ms, st = min(runs, key=lambda t: t[0])
+        out[form] = (ms, int(st.iterations), bool(st.converged))
+        us[form] = d_u.cpu().numpy()
+    del d_a, d_u
+    peak = load_peaks()["hbm_gbs"]
+    prof = ctx.profile_kernels(a, reps=10, tol=TOL, form="mixed")
+    fine = [{"name": r["name"], "us": round(r["avg_ms"] * 1e3, 2),
+             "gbs": round(r["bytes"] / (r["avg_ms"] * 1e-3) / 1e9, 1),
+             "frac": round(r["bytes"] / (r["avg_ms"] * 1e-3) / 1e9 / peak, 3)}
+            for r in prof if r["launches_per_iteration"] > 0 and (r["name"].endswith("(l0)") or "(l" not in r["name"])
+            and r["name"] != "tail_matvec"]
+    err = float(np.linalg.norm(us["mixed"] - us["fp64"]) / np.linalg.norm(us["fp64"]))
+    return {"workload": f"{N_LARGE}x{N_LARGE}, GRF seed 1, a in {{1e3,1e-3}}, f=1, W-cycle, tol 1e-10; "
+                        "one solve per call, device buffers, CUDA events, best of 2",
+            "mixed_ms": round(out["mixed"][0], 2), "fp64_ms": round(out["fp64"][0], 2),
+            "iterations": {"mixed": out["mixed"][1], "fp64": out["fp64"][1]},
+            "converged": {"mixed": out["mixed"][2], "fp64": out["fp64"][2]},
+            "fp64_over_mixed": round(out["fp64"][0] / out["mixed"][0], 3),
+            "mixed_vs_fp64_rel_l2": err,
+            "kernels_mixed": {"note": "the kernels of a CG iteration that touch the finest level, each timed "
+                                      "alone back to back; algorithmic bytes / time against the HBM copy peak "
+                                      "(above 1 where a kernel's own arrays stay in L2 between launches)",
+                              "peak_gbs": peak, "rows": fine}}
 
 
 def run_learned(batch: np.ndarray, pairs: tuple[np.ndarray, np.ndarray], flush) -> dict:
