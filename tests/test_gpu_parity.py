@@ -232,6 +232,24 @@ def test_grid_engine_matches_oracle(darcy, orc, n, cycle) -> None:
     assert got.true_residual <= 2.0 * true_residual(orc, a, want["u"]) + 1e-11
 
 
+@pytest.mark.parametrize("n, cycle, form", [(600, 2, "fp64"), (777, 2, "fp64"), (777, 2, "mixed"), (640, 1, "mixed")])
+def test_grid_engine_large_ragged_sizes(darcy, orc, n, cycle, form) -> None:
+    """Sides between 512 and 1024 that are not powers of two: 600 halves to an
+    odd 75, 777 is odd on every level down to the tail (a one-cell last
+    aggregate in each direction on the 16 x 32-tile levels as well)."""
+    a = two_phase(n, seed=n, hi=1e2, lo=1e-2)
+    oracle_threads(orc, n)
+    want = orc.solve(a, tol=1e-10, cycle_index=cycle)
+    orc.set_threads(1)
+    got = darcy.solve(a, tol=1e-10, cycle_index=cycle, form=form)
+    assert got.converged and got.levels == want["levels"] and got.residual < 1e-10
+    assert rel_l2(got.u, want["u"]) < REL_L2
+    if form == "fp64":
+        assert abs(got.iterations - want["iterations"]) <= max(1, int(0.1 * want["iterations"] + 0.5))
+    else:
+        assert got.iterations <= 1.2 * want["iterations"] + 2
+
+
 @pytest.mark.parametrize("pc", ["jacobi", "none"])
 def test_grid_engine_simple_preconditioners(darcy, orc, pc) -> None:
     a = two_phase(96, seed=2)
@@ -447,6 +465,37 @@ def test_concurrent_grid_solves_report_invalid_input(darcy, monkeypatch) -> None
         ctx.solve_batch(batch_a)
     batch_a[3, 2, 5] = 2.0
     assert ctx.solve_batch(batch_a)["converged"].all()  # the context stays usable
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_host_threads_calling_at_once_get_what_they_get_alone(darcy, form) -> None:
+    """The binding releases the GIL while the GPU works, as the reference's
+    does (src/bindings.cpp:130, :167), so several host threads may call into
+    the package's one context at once. Every call must return exactly what it
+    returns alone -- single solves of several sizes, a batch on the block
+    engine, a batch on concurrent grid-engine solves -- and invalid input must
+    fail only its own call."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    singles = [two_phase(n, seed=400 + q) for q, n in enumerate([48, 64, 128, 400])]
+    small = np.stack([two_phase(64, seed=500 + q) for q in range(16)])
+    large = np.stack([two_phase(384, seed=600 + q) for q in range(3)])
+    bad = np.full((24, 24), 2.0)
+    bad[1, 2] = -1.0
+    jobs = [lambda a=a: darcy.solve(a, tol=1e-10, form=form).u for a in singles]
+    jobs += [lambda: darcy.solve_batch(small, tol=1e-10, form=form).u,
+             lambda: darcy.solve_batch(large, tol=1e-10, form=form).u]
+    alone = [job() for job in jobs]
+
+    def invalid():
+        with pytest.raises(ValueError, match="flat index 26"):
+            darcy.solve(bad, form=form)
+
+    calls = jobs * 3 + [invalid] * 2
+    with ThreadPoolExecutor(max_workers=8) as pool:
+        got = list(pool.map(lambda call: call(), calls))
+    for q, u in enumerate(got[: 3 * len(jobs)]):
+        assert np.array_equal(u, alone[q % len(jobs)]), q % len(jobs)
 
 
 def test_uneven_batch_matches_oracle(darcy, orc) -> None:
