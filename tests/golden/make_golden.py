@@ -117,7 +117,7 @@ def main() -> None:
     record("maxiter2_128", field(128, 0), store_u=False, tol=1e-14, max_iter=2)
     # 1e6 contrast at 64^2 (test_correctness.py:162-170)
     record("contrast1e6_64", field(64, 13, 1e6, 1.0), store_u=True, tol=1e-10, max_iter=2000)
-    # iteration table seed 0 {12,3} (README.md:72-76)
+    # iteration table seed 0 {12,3} (the reference's README.md:72-76)
     for n in (128, 256, 512):
         record(f"table{n}", field(n, 0), tol=1e-10)
     # cfg2 at 1024^2 seed 1, 1e6 contrast
