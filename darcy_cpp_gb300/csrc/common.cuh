@@ -195,30 +195,6 @@ __device__ __forceinline__ void gs_colour(const Lvl<T> L, int c, bool zero) {
     }
 }
 
-// The first red-black sweep from a zero iterate (colour 0 with `zero`, then
-// colour 1) in one pass over all cells. A colour-0 cell is b / d as above; a
-// colour-1 cell reads its colour-0 neighbours as the same rounded products
-// b * (1 / d), formed where they are needed instead of stored and reloaded
-// (the product feeds a multiply, so it is rounded before the multiply-add as
-// the stored value was). Same operations in the same order, same bits as the
-// two passes.
-template <class S, class T>
-__device__ __forceinline__ void gs_first_pair(const Lvl<T> L) {
-    const int n = L.n;
-    const int m = n * n;  // n^2 < 2^31
-    for (int64_t t = S::start(); t < m; t += S::stride()) {
-        const int k = (int)t, i = k / n, j = k - i * n;
-        T v = L.b[k];
-        if ((i + j) & 1) {
-            if (j + 1 < n) v += L.e[k] * (L.b[k + 1] * L.id[k + 1]);
-            if (j > 0) v += L.e[k - 1] * (L.b[k - 1] * L.id[k - 1]);
-            if (i + 1 < n) v += L.nf[k] * (L.b[k + n] * L.id[k + n]);
-            if (i > 0) v += L.nf[k - n] * (L.b[k - n] * L.id[k - n]);
-        }
-        L.x[k] = v * L.id[k];
-    }
-}
-
 // Residual of one cell, r = b - A x (level.hpp:122-137).
 template <class T>
 __device__ __forceinline__ T cell_residual(const Lvl<T>& L, int i, int j) {

@@ -112,10 +112,6 @@ void launch_cg_init(const double* f, double h2, int64_t m, double* b, double* r,
                     cudaStream_t s);
 template <class T>
 void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t s);
-// The first red-black sweep of a level from a zero iterate, both colours in
-// one launch (gs_first_pair).
-template <class T>
-void launch_gs_first_pair(const Lvl<T>& L, CgState* st, cudaStream_t s);
 template <class T>
 void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s);
 void launch_residual_restrict_df(const Lvl<float>& L, const float* elo, const float* nlo, const float* dlo,

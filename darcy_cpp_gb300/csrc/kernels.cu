@@ -204,12 +204,6 @@ __global__ void k_gs(Lvl<T> L, int c, bool zero, const CgState* st) {
     gs_colour<GridScope>(L, c, zero);
 }
 template <class T>
-__global__ void k_gs_first_pair(Lvl<T> L, const CgState* st) {
-    pdl_enter();
-    if (st && st->done) return;
-    gs_first_pair<GridScope>(L);
-}
-template <class T>
 __global__ void k_residual_restrict(Lvl<T> L, T* bc, const CgState* st) {
     pdl_enter();
     if (st && st->done) return;
@@ -831,10 +825,6 @@ void launch_gs(const Lvl<T>& L, int colour, bool zero, CgState* st, cudaStream_t
     launch_k(k_gs<T>, grid_fill(k_gs<T>, colour_count(L.n, colour)), kThreads, 0, s, L, colour, zero, st);
 }
 template <class T>
-void launch_gs_first_pair(const Lvl<T>& L, CgState* st, cudaStream_t s) {
-    launch_k(k_gs_first_pair<T>, grid_fill(k_gs_first_pair<T>, (int64_t)L.n * L.n), kThreads, 0, s, L, st);
-}
-template <class T>
 void launch_residual_restrict(const Lvl<T>& L, T* bc, CgState* st, cudaStream_t s) {
     const int64_t nc = (L.n + 1) / 2;
     launch_k(k_residual_restrict<T>, grid_fill(k_residual_restrict<T>, nc * nc), kThreads, 0, s, L, bc, st);
@@ -1187,7 +1177,6 @@ void launch_block_solve(const BatchArgs& args, int ctas, int threads, cudaStream
 
 #define DGPU_INSTANTIATE(T)                                                                                \
     template void launch_gs<T>(const Lvl<T>&, int, bool, CgState*, cudaStream_t);                          \
-    template void launch_gs_first_pair<T>(const Lvl<T>&, CgState*, cudaStream_t);                   \
     template void launch_residual_restrict<T>(const Lvl<T>&, T*, CgState*, cudaStream_t);                  \
     template void launch_prolong_gs1<T>(const Lvl<T>&, const T*, CgState*, cudaStream_t);                  \
     template void launch_gs0_dot<T>(const Lvl<T>&, const double*, CgState*, double*, cudaStream_t);        \

@@ -417,12 +417,8 @@ void emit_visit(GridPlan& P, int l, bool first, cudaStream_t s) {
     const PlanKey& K = P.key;
     const Lvl<T>& A = lv[l];
     for (int q = 0; q < K.pre; ++q) {
-        if (first && q == 0) {
-            launch_gs_first_pair<T>(A, P.st, s);
-        } else {
-            launch_gs<T>(A, 0, false, P.st, s);
-            launch_gs<T>(A, 1, false, P.st, s);
-        }
+        launch_gs<T>(A, 0, first && q == 0, P.st, s);
+        launch_gs<T>(A, 1, false, P.st, s);
     }
     if constexpr (sizeof(T) == 4)  // the FP32 cycle restricts a double-float residual
         launch_residual_restrict_df(A, P.elo[l], P.nlo[l], P.dlo[l], l == 0 ? P.b0lo : nullptr, lv[l + 1].b, P.st,
@@ -544,12 +540,8 @@ void emit_visit_hybrid(GridPlan& P, int l, bool first, std::vector<int>& cur, cu
     const auto& lv = levels_of<T>(P);
     const PlanKey& K = P.key;
     const Lvl<T>& A = lv[l];
-    if (first) {
-        launch_gs_first_pair<T>(A, P.st, s);
-    } else {
-        launch_gs<T>(A, 0, false, P.st, s);
-        launch_gs<T>(A, 1, false, P.st, s);
-    }
+    launch_gs<T>(A, 0, first, P.st, s);
+    launch_gs<T>(A, 1, false, P.st, s);
     if constexpr (sizeof(T) == 4)
         launch_residual_restrict_df(A, P.elo[l], P.nlo[l], P.dlo[l], l == 0 ? P.b0lo : nullptr, lv[l + 1].b, P.st,
                                     s);
@@ -1930,8 +1922,9 @@ int dgpu_profile_kernels(dgpu_context* ctx, const double* a, int64_t n, const dg
                                      launch_visit_post<T>(V0, xa, x1, xb, rvec, stp, partials, s);
                                  }});
             }
-            // b, 1/d, e, nf read and x written once per cell
-            items.push_back({"gs_first_pair(l0)", w * 5 * m, on_u, [=] { launch_gs_first_pair<T>(L0, stp, s); }});
+            items.push_back({"gs_colour0_zero(l0)", w * m * 1.5, on_u, [=] { launch_gs<T>(L0, 0, true, stp, s); }});
+            items.push_back({"gs_colour1(l0)", w * (m * 0.5 * 3 + m * 2 + m), on_u,
+                             [=] { launch_gs<T>(L0, 1, false, stp, s); }});
             if constexpr (sizeof(T) == 4) {  // double-float: e, nf, d and their lo parts, x, b, b_lo
                 const float *elo = P.elo[0], *nlo = P.nlo[0], *dlo = P.dlo[0], *blo = P.b0lo;
                 items.push_back({"residual_restrict(l0)", w * (8 * m + mc) + 4 * m, on_u, [=] {
