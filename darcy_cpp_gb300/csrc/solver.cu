@@ -1240,17 +1240,18 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         cfg.threads = hit->second.threads;
         cfg.smem = hit->second.smem;
     } else if (count >= C->sms) {
-        // time every candidate on the batch itself (its largest problems when
-        // it holds more than 32 per SM): which shape wins depends on how the
-        // count divides into waves of resident problems. 4096 x 64^2 FP64:
-        // 128 threads and no shared-memory budget (8 CTAs per SM) 43.0 ms, 256
-        // threads and 48 KiB (4 per SM) 41.1 ms; on 3648 of those problems
-        // 36.0 against 37.6 ms, on 1216 12.1 against 12.4 ms -- so samples of
-        // 8 and 24 per SM had chosen the slower shape for the full batch. (A
-        // sample of 2 per SM had likewise hidden what 4 CTAs of 256 threads
-        // gain: 512 threads chosen at 174.5K / 88.6K solves/s mixed / FP64
-        // against 180.9K / 96.4K with 256.)
-        const int64_t sample = std::min<int64_t>(count, 32 * (int64_t)C->sms);
+        // time every candidate on the batch's largest problems, 8 per SM: a
+        // sample of 2 per SM hid what 4 CTAs of 256 threads gain on a full
+        // batch (4096 x 64^2: 512 threads chosen at 174.5K solves/s mixed,
+        // 88.6K FP64, against 180.9K and 96.4K with 256). Which shape wins
+        // also depends on how the count divides into waves of resident
+        // problems, and the host path runs large batches in chunks of other
+        // counts, so no sample is exact: 4096 x 64^2 FP64 takes 43.0 ms with
+        // the 128 threads chosen here and 41.1 ms with 256 threads and 48 KiB,
+        // which win at 4096 problems but not at 3648; tuning on the whole batch chose
+        // worse shapes for the uneven sides 32..256 (19.8K against 21.2K
+        // solves/s mixed) and cost 8 s.
+        const int64_t sample = std::min<int64_t>(count, 8 * (int64_t)C->sms);
         float best = 1e30f;
         // (1024 threads: one problem per SM, half the resident arenas of 2 x 512,
         // for when the arenas of all resident problems outgrow the L2)
@@ -1263,10 +1264,9 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         for (int threads : {128, 256, 512, 1024}) {
             add(threads, 0);
             add(threads, smem_budget_for(mixed));
-            // 48 KiB for both forms: the FP64 form's own budget (96 KiB) leaves
-            // 2 CTAs per SM, none 4; 4096 x 64^2 FP64 measured 95.3K solves/s
-            // with the shape chosen without it (128 threads, no budget) and
-            // 99.4K with 256 threads and 48 KiB
+            // 48 KiB for both forms (the FP64 form's own 96 KiB leaves 2 CTAs
+            // per SM): 4096 uneven sides 32..256 FP64, 512 threads, 14.2K
+            // solves/s against 13.6K with 96 KiB
             if (threads <= 512) add(threads, 48 * 1024);
             if (threads == 1024) add(threads, 96 * 1024);
             if (mixed && threads >= 512) add(threads, kSmemBudgetLarge);
