@@ -1245,12 +1245,10 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         // batch (4096 x 64^2: 512 threads chosen at 174.5K solves/s mixed,
         // 88.6K FP64, against 180.9K and 96.4K with 256). Which shape wins
         // also depends on how the count divides into waves of resident
-        // problems, and the host path runs large batches in chunks of other
-        // counts, so no sample is exact: 4096 x 64^2 FP64 takes 43.0 ms with
-        // the 128 threads chosen here and 41.1 ms with 256 threads and 48 KiB,
-        // which win at 4096 problems but not at 3648; tuning on the whole batch chose
-        // worse shapes for the uneven sides 32..256 (19.8K against 21.2K
-        // solves/s mixed) and cost 8 s.
+        // problems, so no sample is exact (the full-batch check below);
+        // timing every candidate on the whole batch chose worse shapes for
+        // the uneven sides 32..256 (19.8K against 21.2K solves/s mixed) and
+        // cost 8 s.
         const int64_t sample = std::min<int64_t>(count, 8 * (int64_t)C->sms);
         float best = 1e30f;
         // (1024 threads: one problem per SM, half the resident arenas of 2 x 512,
@@ -1282,24 +1280,47 @@ void block_solve(dgpu_context* C, int64_t count, const std::vector<int>& sides, 
         // kTuneLaunchMs, tuning would cost more than it can save: keep the
         // default.
         constexpr float kTuneLaunchMs = 150.f;
-        for (size_t ci = 0; ci < cands.size(); ++ci) {
-            const BlockConfig c = cands[ci];
-            launch(c, sample);  // warm (allocations, clocks)
+        auto time_on = [&](const BlockConfig& c, int64_t n_prob) {
+            launch(c, n_prob);  // warm (allocations, clocks)
             float ms = 1e30f;
             for (int rep = 0; rep < 2; ++rep) {  // best of two: one timing let noise pick the shape
                 CK(cudaEventRecord(C->ev0, s));
-                launch(c, sample);
+                launch(c, n_prob);
                 CK(cudaEventRecord(C->ev1, s));
                 CK(cudaEventSynchronize(C->ev1));
                 float t = 0.f;
                 CK(cudaEventElapsedTime(&t, C->ev0, C->ev1));
                 ms = std::min(ms, t);
             }
+            return ms;
+        };
+        std::vector<std::pair<float, BlockConfig>> timed;
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+            const float ms = time_on(cands[ci], sample);
+            timed.emplace_back(ms, cands[ci]);
             if (ms < best) {
                 best = ms;
-                cfg = c;
+                cfg = cands[ci];
             }
             if (ci == 0 && ms > kTuneLaunchMs) break;
+        }
+        // The three fastest on the sample are timed again on the whole batch
+        // when its launch is short (estimated from the sample at under
+        // kFullCheckMs): 4096 x 64^2 FP64 then takes 256 threads and 48 KiB
+        // (41.1 ms) over the sample's choice of 128 threads without a budget
+        // (43.0 ms), which wins only on fewer problems.
+        constexpr float kFullCheckMs = 80.f;
+        if (count > sample && timed.size() > 1 && best * (float)count / (float)sample < kFullCheckMs) {
+            std::sort(timed.begin(), timed.end(),
+                      [](const auto& x, const auto& y) { return x.first < y.first; });
+            float best_full = 1e30f;
+            for (size_t k = 0; k < std::min<size_t>(3, timed.size()); ++k) {
+                const float ms = time_on(timed[k].second, count);
+                if (ms < best_full) {
+                    best_full = ms;
+                    cfg = timed[k].second;
+                }
+            }
         }
         C->tuned[key] = BlockConfigPOD{cfg.threads, cfg.smem};
         save_tuning(C);
