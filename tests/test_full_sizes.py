@@ -104,11 +104,8 @@ def test_combined_16384x128_plus_64x512(darcy, orc) -> None:
     err = np.linalg.norm((np.stack(mixed.u[:16384]) - small_u).reshape(16384, -1), axis=1)
     assert (err < REL_L2 * np.linalg.norm(small_u.reshape(16384, -1), axis=1)).all()
     assert max(rel_l2(mixed.u[q], fp64.u[q]) for q in range(16384, len(big))) < REL_L2
-    orc.set_threads(min(16, orc.cpu_count()))
-    try:
-        for q in [0, 9999, 16384]:
-            want = orc.solve(big[q], tol=1e-10)
-            assert abs(int(fp64.iterations[q]) - want["iterations"]) <= max(1, round(0.1 * want["iterations"]))
-            assert rel_l2(fp64.u[q], want["u"]) < REL_L2
-    finally:
-        orc.set_threads(1)
+    orc.set_threads(1)  # deterministic: several threads combine the dot products in arrival order
+    for q in [0, 9999, 16384]:
+        want = orc.solve(big[q], tol=1e-10)
+        assert abs(int(fp64.iterations[q]) - want["iterations"]) <= max(1, round(0.1 * want["iterations"]))
+        assert rel_l2(fp64.u[q], want["u"]) < REL_L2
