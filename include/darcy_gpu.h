@@ -109,17 +109,18 @@ int dgpu_solve_device(dgpu_context* ctx, const double* d_a, const double* d_f, d
 /* _core.solve_batch, reference src/bindings.cpp:140-197: `batch` problems of
  * one side n, packed (batch, n, n). f: NULL (f_scalar), one n*n array shared
  * by every sample (f_per_sample = 0, the reference's behaviour) or a packed
- * (batch, n, n) array (f_per_sample = 1). Outputs per sample. levels may be NULL. */
+ * (batch, n, n) array (f_per_sample = 1). Outputs per sample. levels may be NULL.
+ * Problems of side >= 384 run as up to four concurrent single solves (one
+ * plan and stream each), smaller ones as one launch with one problem per CTA. */
 int dgpu_solve_batch(dgpu_context* ctx, const double* a, const double* f, double f_scalar, int f_per_sample,
                      int64_t batch, int64_t n, const dgpu_options* opt, const double* u0, double* u_out,
                      int* iterations, double* residuals, int* converged, int* levels);
 
 /* Same, on device-resident arrays (d_a, d_f, d_u0, d_u: device pointers,
  * packed as above); per-sample results in host arrays; device_ms (may be
- * NULL) receives the device time of the solve. Problems too large for one
- * CTA's share of the batch run as concurrent grid-engine solves, one stream
- * each. Ordered after `stream` (may be
- * NULL); returns when the results are written. No reference counterpart. */
+ * NULL) receives the device time of the solve. Routed as dgpu_solve_batch.
+ * Ordered after `stream` (may be NULL); returns when the results are written.
+ * No reference counterpart. */
 int dgpu_solve_batch_device(dgpu_context* ctx, const double* d_a, const double* d_f, double f_scalar,
                             int f_per_sample, int64_t batch, int64_t n, const dgpu_options* opt, const double* d_u0,
                             double* d_u, int* iterations, double* residuals, int* converged, int* levels,
@@ -131,7 +132,9 @@ int64_t dgpu_last_launches(const dgpu_context* ctx);
 
 /* Uneven-size batch (additive extension of solve_batch): problem p has side
  * sides[p] and occupies cells [off_p, off_p + sides[p]^2) of the packed
- * arrays, off_p being the running sum. f/u0 follow the same packing or NULL. */
+ * arrays, off_p being the running sum. f/u0 follow the same packing or NULL.
+ * Each problem is routed as in dgpu_solve_batch: the small ones share one
+ * launch, those of side >= 384 follow as concurrent single solves. */
 int dgpu_solve_uneven(dgpu_context* ctx, int64_t count, const int64_t* sides, const double* a,
                       const double* f, double f_scalar, const dgpu_options* opt, const double* u0,
                       double* u_out, int* iterations, double* residuals, int* converged, int* levels);
